@@ -1,0 +1,206 @@
+"""ctypes loader for the CPU restatement (liboracle_strip.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` -- never by the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle_strip.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+
+class OrcGeom(C.Structure):
+    _fields_ = [
+        ("radius", C.c_double),
+        ("scintillator_length", C.c_double),
+        ("n_y_pixels", C.c_int32),
+        ("n_z_pixels", C.c_int32),
+        ("pixel_height", C.c_double),
+        ("pixel_width", C.c_double),
+        ("sigma_z", C.c_double),
+        ("sigma_dl", C.c_double),
+    ]
+
+
+class OrcStats(C.Structure):
+    _fields_ = [
+        ("n_events", C.c_int64),
+        ("n_pixels", C.c_int64),
+        ("n_kernel_calls", C.c_int64),
+        ("n_contributing", C.c_int64),
+    ]
+
+
+@dataclass
+class Geometry:
+    radius: float
+    length: float
+    n_y: int
+    n_z: int
+    pixel: float
+    sigma_z: float
+    sigma_dl: float
+
+    def c(self) -> OrcGeom:
+        return OrcGeom(self.radius, self.length, self.n_y, self.n_z, self.pixel,
+                       self.pixel, self.sigma_z, self.sigma_dl)
+
+
+def build() -> str:
+    """Compiles the restatement with make (seconds); returns the library path."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        gp = C.POINTER(OrcGeom)
+        fp = C.POINTER(C.c_float)
+        L.orc_mlem_f.argtypes = [gp, f32p, C.c_int64, f32p, C.c_int, C.c_int, C.POINTER(OrcStats)]
+        L.orc_mlem_d.argtypes = [gp, f32p, C.c_int64, f64p, C.c_int, C.c_int, C.POINTER(OrcStats)]
+        L.orc_mlem_gpuref.argtypes = [gp, f32p, C.c_int64, f32p, C.c_int, C.c_int, C.c_void_p]
+        L.orc_sensitivity_map_f.argtypes = [gp, C.c_int, f32p]
+        L.orc_nll_grad.argtypes = [gp, C.c_double, C.c_double, f32p, C.c_int64, f32p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                   C.POINTER(C.c_int64)]
+        L.orc_nll_grad.restype = C.c_double
+        L.orc_gaussian_kernel_f.argtypes = [C.c_float] * 8
+        L.orc_gaussian_kernel_f.restype = C.c_float
+        L.orc_gaussian_kernel_d.argtypes = [C.c_double] * 8
+        L.orc_gaussian_kernel_d.restype = C.c_double
+        L.orc_analytic_kernel_d.argtypes = [C.c_double] * 8
+        L.orc_analytic_kernel_d.restype = C.c_double
+        L.orc_analytic_kernel_f.argtypes = [C.c_float] * 8
+        L.orc_analytic_kernel_f.restype = C.c_float
+        L.orc_bb_y_dd.argtypes = [C.c_double] * 3
+        L.orc_bb_y_dd.restype = C.c_double
+        L.orc_bb_z_dd.argtypes = [C.c_double] * 3
+        L.orc_bb_z_dd.restype = C.c_double
+        L.orc_sensitivity_d.argtypes = [gp, C.c_double, C.c_double]
+        L.orc_sensitivity_d.restype = C.c_double
+        L.orc_pixel_at_d.argtypes = [gp, C.c_double, C.c_double, C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32)]
+        L.orc_pixel_center_d.argtypes = [gp, C.c_int32, C.c_int32, C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double)]
+        L.orc_response_tan_y_z_f.argtypes = [C.c_float] * 4 + [fp] * 3
+        L.orc_ellipse_bb_f.argtypes = [C.c_float] * 3 + [fp] * 6
+        L.orc_event_box_f.argtypes = [gp, C.c_float, C.c_float, C.c_float] + [C.POINTER(C.c_int32)] * 4
+        L.orc_event_box_f.restype = C.c_int32
+        L.orc_to_projection_space_tan_d.argtypes = [C.c_double] * 4 + [C.POINTER(C.c_double)] * 3
+        _lib = L
+    return _lib
+
+
+def _events(ev) -> np.ndarray:
+    ev = np.ascontiguousarray(ev, dtype=np.float32).reshape(-1, 3)
+    return ev
+
+
+def mlem_f(geom: Geometry, events, n_iterations: int, rho=None, threads: int = 1):
+    """Reference CPU float path: returns (rho float32[n_y, n_z], stats dict)."""
+    ev = _events(events)
+    r = (np.ones(geom.n_y * geom.n_z, np.float32) if rho is None
+         else np.ascontiguousarray(rho, np.float32).reshape(-1).copy())
+    st = OrcStats()
+    g = geom.c()
+    rc = lib().orc_mlem_f(C.byref(g), ev.reshape(-1), len(ev), r, n_iterations, threads,
+                          C.byref(st))
+    if rc != 0:
+        raise RuntimeError("orc_mlem_f failed")
+    return r.reshape(geom.n_y, geom.n_z), dict(
+        n_events=st.n_events, n_pixels=st.n_pixels, n_kernel_calls=st.n_kernel_calls,
+        n_contributing=st.n_contributing)
+
+
+def mlem_d(geom: Geometry, events, n_iterations: int, rho=None, threads: int = 0):
+    """FP64 instantiation of the same algorithm; returns float64[n_y, n_z]."""
+    ev = _events(events)
+    r = (np.ones(geom.n_y * geom.n_z, np.float64) if rho is None
+         else np.ascontiguousarray(rho, np.float64).reshape(-1).copy())
+    st = OrcStats()
+    g = geom.c()
+    rc = lib().orc_mlem_d(C.byref(g), ev.reshape(-1), len(ev), r, n_iterations, threads,
+                          C.byref(st))
+    if rc != 0:
+        raise RuntimeError("orc_mlem_d failed")
+    return r.reshape(geom.n_y, geom.n_z)
+
+
+def mlem_gpuref(geom: Geometry, events, n_iterations: int, rho=None, threads: int = 0):
+    """Reference GPU-kernel semantics (analytic kernel, sensitivity-weighted denominator)."""
+    ev = _events(events)
+    r = (np.ones(geom.n_y * geom.n_z, np.float32) if rho is None
+         else np.ascontiguousarray(rho, np.float32).reshape(-1).copy())
+    g = geom.c()
+    rc = lib().orc_mlem_gpuref(C.byref(g), ev.reshape(-1), len(ev), r, n_iterations,
+                               threads, None)
+    if rc != 0:
+        raise RuntimeError("orc_mlem_gpuref failed")
+    return r.reshape(geom.n_y, geom.n_z)
+
+
+def sensitivity_map(geom: Geometry, kind: int = 0) -> np.ndarray:
+    out = np.empty(geom.n_y * geom.n_z, np.float32)
+    g = geom.c()
+    lib().orc_sensitivity_map_f(C.byref(g), kind, out)
+    return out.reshape(geom.n_y, geom.n_z)
+
+
+def nll_grad(geom: Geometry, events, rho, support_sigma=None, s=None, threads: int = 0,
+             want_grad_rho: bool = True):
+    """FP64 NLL, dL/drho (float64 image) and dL/dsigma (float64[2])."""
+    ev = _events(events)
+    r = np.ascontiguousarray(rho, np.float32).reshape(-1)
+    g = geom.c()
+    ssz, ssdl = support_sigma if support_sigma is not None else (geom.sigma_z, geom.sigma_dl)
+    gr = np.zeros(r.size, np.float64) if want_grad_rho else None
+    gs = np.zeros(2, np.float64)
+    s_arr = None if s is None else np.ascontiguousarray(s, np.float32).reshape(-1)
+    skipped = C.c_int64(0)
+    loss = lib().orc_nll_grad(
+        C.byref(g), ssz, ssdl, ev.reshape(-1), len(ev), r,
+        None if s_arr is None else s_arr.ctypes.data,
+        None if gr is None else gr.ctypes.data, gs.ctypes.data, threads, C.byref(skipped))
+    return loss, (None if gr is None else gr.reshape(geom.n_y, geom.n_z)), gs, skipped.value
+
+
+def gaussian_kernel_f(sz, sdl, y, tan, sec, R, dz, dy) -> float:
+    return lib().orc_gaussian_kernel_f(sz, sdl, y, tan, sec, R, dz, dy)
+
+
+def gaussian_kernel_d(sz, sdl, y, tan, sec, R, dz, dy) -> float:
+    return lib().orc_gaussian_kernel_d(sz, sdl, y, tan, sec, R, dz, dy)
+
+
+def analytic_kernel_d(sz, sdl, y, tan, sec, R, dz, dy) -> float:
+    return lib().orc_analytic_kernel_d(sz, sdl, y, tan, sec, R, dz, dy)
+
+
+def event_box(geom: Geometry, z_u, z_d, dl):
+    vals = [C.c_int32() for _ in range(4)]
+    g = geom.c()
+    cnt = lib().orc_event_box_f(C.byref(g), z_u, z_d, dl, *[C.byref(v) for v in vals])
+    return tuple(v.value for v in vals), cnt
+
+
+def ref_binary(name: str) -> str | None:
+    """Path of a reference tool built by build_ref.sh, if present on this host."""
+    p = os.path.join(REF_DIR, name)
+    return p if os.path.exists(p) and os.access(p, os.X_OK) else None
