@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 strip-PET list-mode TOF MLEM iteration.
+
+One step = one MLEM iteration over every event of the workload (default: the
+full-size plain case, 500 x 450 pixels at 2 mm, 2e7 events from a seeded
+10-ellipse phantom).  Prints one JSON line.
+
+  value   event-iterations/s with the events already prepared in HBM (device
+          time of K iterations, CUDA events on the library's stream)
+  e2e     the same metric through the C ABI with host buffers: each e2e step
+          uploads the events from pinned host memory, prepares them, runs the
+          workload's iteration count from a uniform image and reads the image
+          back (jpet_strip_run's work), timed on the host
+  roofline  kernel-pixel evaluations/s against the measured ex2 (SFU) rate:
+          the iteration evaluates one exp per in-ellipse pixel
+  cpu_baseline  the CPU restatement of the reference's OpenMP path on this
+          host's cores, on a bounded sample of the same events
+
+--impl reference times that CPU path alone (the reference GPU backend does not
+compile with CUDA >= 12, so the reference's CPU float path is the reference).
+Multi-GPU (torchrun): every rank runs an independent replica (the path has no
+exchange step); value is the sum over ranks / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "j-pet-mlem_gb300")
+sys.path.insert(0, os.path.join(PKG, "python"))
+
+METRIC = ("event·iterations/sec and kernel-pixel evals/sec at stated L2 tol vs FP64; "
+          "% SFU/atomic roofline")
+UNIT = "event·iterations/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="plain-2mm-20M")
+    p.add_argument("--events", type=int, default=0, help="override the event count")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(device), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax),
+                "power_w_max": max(power), "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks(device: int):
+    lib = C.CDLL(os.path.join(PKG, "lib", "libjpet_peaks.so"))
+    out = (C.c_double * 6)()
+    rc = lib.jpet_peaks_measure(device, out)
+    if rc != 0:
+        raise RuntimeError(f"peak microbenchmark failed: {rc}")
+    return {"ex2_per_s": out[0], "ffma_per_s": out[1], "shared_atomic_per_s": out[2],
+            "global_atomic_per_s": out[3], "sms": int(out[4]), "sm_clock_khz": int(out[5])}
+
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_sample_rate(wl, events, budget_s: float, threads: int):
+    """Times the CPU restatement of the reference's OpenMP path (one iteration
+    from a uniform image) on a prefix of the events sized to ~budget_s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    og = oracle.Geometry(*wl.geometry_args())
+    probe = min(len(events), 20000)
+    t = time.perf_counter()
+    oracle.mlem_f(og, events[:probe], 1, threads=threads)
+    dt = max(time.perf_counter() - t, 1e-3)
+    n = int(min(len(events), max(probe, probe * budget_s / dt)))
+    t = time.perf_counter()
+    _, st = oracle.mlem_f(og, events[:n], 1, threads=threads)
+    dt = time.perf_counter() - t
+    return n, dt, st
+
+
+def reference_arm(args, wl, world, rank):
+    if rank != 0:
+        return
+    import numpy as np
+
+    threads = os.cpu_count() or 1
+    n_all = args.events or wl.n_events
+    # sample sized so that each step is a few seconds of the CPU path
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    probe_ev = wl.events(min(n_all, 20000))
+    og = oracle.Geometry(*wl.geometry_args())
+    t = time.perf_counter()
+    oracle.mlem_f(og, probe_ev, 1, threads=threads)
+    rate = len(probe_ev) / max(time.perf_counter() - t, 1e-3)
+    budget = max(2.0, 120.0 / max(1, args.steps + args.warmup))
+    n = int(min(n_all, max(len(probe_ev), rate * budget)))
+    ev = wl.events(n)
+    rho = None
+    for _ in range(args.warmup):
+        rho, _ = oracle.mlem_f(og, ev, 1, rho, threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        rho, st = oracle.mlem_f(og, ev, 1, rho, threads=threads)
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    value = n * args.steps / total
+    evals = st["n_kernel_calls"]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl.name, "events": n_all, "grid": f"{wl.n_z}x{wl.n_y}",
+                   "pixel_mm": wl.pixel, "sigma_z": wl.sigma_z, "sigma_dl": wl.sigma_dl},
+        "kernel_pixel_evals_per_s": evals * args.steps / total,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"first {n} of {n_all} events, one iteration per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def gb300_arm(args, wl, world, rank, local):
+    import numpy as np
+    import torch
+
+    from jpet_strip import capi
+
+    torch.cuda.set_device(local)
+    if world > 1 and not torch.distributed.is_initialized():
+        torch.distributed.init_process_group("nccl")
+    n_events = args.events or wl.n_events
+    events = wl.events(n_events)
+    geom = capi.Geometry(*wl.geometry_args())
+    peaks = measured_peaks(local)
+    stream = torch.cuda.Stream()
+    rec = capi.StripReconstruction(geom, device=local)
+    rec.set_stream(stream.cuda_stream)
+    rec.set_events(events)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            rec.iterate(1)
+    rec.synchronize()
+    counters = rec.counters()
+    evals_per_iter = counters["n_kernel_calls"]
+    launches_per_iter = 1 + (1 if counters["n_oversize"] > 0 else 0)
+
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for k in range(args.steps):
+        starts[k].record(stream)
+        rec.iterate(1)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    per_step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = starts[0].elapsed_time(ends[-1])
+    t_max = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t_max, op=torch.distributed.ReduceOp.MAX)
+    total_ms = float(t_max.item())
+    value = world * n_events * args.steps / (total_ms * 1e-3)
+    kernel_ms = statistics.mean(per_step_ms)
+    evals_per_s = evals_per_iter / (kernel_ms * 1e-3)
+
+    # accuracy on a sample: one iteration vs the float and FP64 oracles
+    accuracy = None
+    cpu = None
+    if rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        og = oracle.Geometry(*wl.geometry_args())
+        sample = events[:200000]
+        with capi.StripReconstruction(geom, device=local) as r2:
+            r2.set_events(sample)
+            r2.iterate(1)
+            got = r2.rho.astype(np.float64)
+        f32, _ = oracle.mlem_f(og, sample, 1, threads=os.cpu_count() or 1)
+        f64 = oracle.mlem_d(og, sample, 1, threads=os.cpu_count() or 1)
+        accuracy = {
+            "sample_events": len(sample), "iterations": 1,
+            "rel_l2_vs_reference_float": float(np.linalg.norm(got - f32) / np.linalg.norm(f32)),
+            "rel_l2_vs_fp64": float(np.linalg.norm(got - f64) / np.linalg.norm(f64)),
+            "reference_float_rel_l2_vs_fp64": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
+            "tolerance": 1e-5,
+        }
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            n, dt, st = cpu_sample_rate(wl, events, args.cpu_seconds, threads)
+            cpu = {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"first {n} of {n_events} events, one iteration from a uniform image",
+                   "kernel_pixel_evals_per_s": st["n_kernel_calls"] / dt}
+
+    # end to end through the C ABI with host buffers (pinned)
+    pinned = torch.empty((n_events, 3), dtype=torch.float32, pin_memory=True)
+    pinned.numpy()[:] = events
+    ones = np.ones((wl.n_y, wl.n_z), np.float32)
+    e2e_times = []
+    host_img = None
+    for k in range(args.e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rec.set_events(pinned.numpy())
+        rec.rho = ones
+        rec.iterate(wl.iterations)
+        host_img = rec.rho
+        t1 = time.perf_counter()
+        if k > 0:
+            e2e_times.append(t1 - t0)
+    e2e_s = max(e2e_times) if world == 1 else max(e2e_times)
+    e2e_value = world * n_events * wl.iterations / (sum(e2e_times) / len(e2e_times))
+    rec.close()
+
+    if rank != 0:
+        return
+    hbm, hbm_kind = hbm_peak()
+    ex2_peak = peaks["ex2_per_s"]
+    atom_frac = evals_per_s / peaks["shared_atomic_per_s"]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl.name, "events": n_events, "grid": f"{wl.n_z}x{wl.n_y}",
+                   "pixel_mm": wl.pixel, "sigma_z": wl.sigma_z, "sigma_dl": wl.sigma_dl,
+                   "phantom": wl.phantom, "seed": wl.seed,
+                   "l2": "inputs larger than L2 (prepared events 24 B each)",
+                   "parallelism": f"replicas{world}"},
+        "kernel_pixel_evals_per_s": world * evals_per_s,
+        "evals_per_event": evals_per_iter / n_events,
+        "roofline": {"bound": "sfu", "achieved": evals_per_s / 1e9, "peak": ex2_peak / 1e9,
+                     "unit": "Gex2/s", "frac": evals_per_s / ex2_peak,
+                     "peak_source": "measured ex2.approx rate on this GPU (libjpet_peaks)",
+                     "shared_atomic_frac": atom_frac,
+                     "traffic": None, "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_kind},
+        "accuracy": accuracy,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": int(12 * n_events + 4 * wl.n_y * wl.n_z),
+                "d2h_bytes_per_step": int(4 * wl.n_y * wl.n_z),
+                "iterations_per_step": wl.iterations, "seconds_per_step": e2e_s},
+        "gpu_launches": launches_per_iter * args.steps,
+        "clocks": clk,
+        "peaks": peaks,
+        "counters": counters,
+        "kernel_ms_per_iteration": kernel_ms,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    from jpet_strip.workloads import WORKLOADS
+
+    wl = WORKLOADS[args.workload]
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, wl, world, rank)
+    else:
+        gb300_arm(args, wl, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

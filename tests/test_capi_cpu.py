@@ -1,0 +1,77 @@
+"""C-ABI checks that need no GPU: the library builds, loads and exports every
+symbol include/jpet_strip.h declares; argument errors are reported as status
+codes without touching a device."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from jpet_strip import capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))
+           if f.endswith(".h")]
+
+
+def _declared():
+    names = set()
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(jpet_\w+)\s*\(", text):
+            names.add(m.group(1))
+        for m in re.finditer(r"typedef\s+\w+\s*\(\*\s*(jpet_\w+)\)", text):
+            names.discard(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_and_library_exports_every_symbol():
+    L = capi.lib()
+    declared = _declared()
+    assert declared, "no declarations found"
+    missing = [n for n in declared if not hasattr(L, n)]
+    assert not missing, missing
+    assert set(capi.EXPORTED) >= set(n for n in declared if n.startswith("jpet_strip"))
+
+
+def test_abi_version_and_defaults():
+    L = capi.lib()
+    assert L.jpet_strip_abi_version() == 1
+    o = capi.make_opts()
+    assert o.mode == capi.MODE_CPU_REFERENCE and o.precision == capi.PRECISION_FP32
+    assert all(v == 0 for v in o.reserved)
+
+
+def test_create_rejects_bad_geometry_without_device():
+    L = capi.lib()
+    h = C.c_void_p()
+    g = capi.Geometry(450, 1000, 0, 200, 5, 10, 42).c()
+    rc = L.jpet_strip_create(C.byref(g), None, C.byref(h))
+    assert rc == capi.JPET_ERR_ARGUMENT
+    assert b"n_y_pixels" in L.jpet_strip_last_error(None)
+    g = capi.Geometry(450, 1000, 180, 200, -5, 10, 42).c()
+    assert L.jpet_strip_create(C.byref(g), None, C.byref(h)) == capi.JPET_ERR_ARGUMENT
+    assert L.jpet_strip_create(C.byref(g), None, None) == capi.JPET_ERR_ARGUMENT
+    assert L.jpet_strip_destroy(None) == 0
+
+
+def test_null_handle_calls_are_argument_errors():
+    L = capi.lib()
+    for fn, args in [(L.jpet_strip_iterate, (None, 1)), (L.jpet_strip_get_image, (None, None)),
+                     (L.jpet_strip_set_events, (None, None, 0)),
+                     (L.jpet_strip_synchronize, (None,))]:
+        assert fn(*args) == capi.JPET_ERR_ARGUMENT
+
+
+def test_no_device_is_a_status_not_an_abort():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    L = capi.lib()
+    h = C.c_void_p()
+    g = capi.Geometry(450, 1000, 180, 200, 5, 10, 42).c()
+    rc = L.jpet_strip_create(C.byref(g), None, C.byref(h))
+    assert rc == capi.JPET_ERR_CUDA
+    assert not h.value

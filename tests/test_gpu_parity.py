@@ -1,0 +1,221 @@
+"""Parity of the sm_103a MLEM iteration (through the C ABI) with the CPU oracle.
+
+Tolerances: per-iteration relative L2 <= 1e-5 against the reference float path
+(the bar the path is built to), <= 1e-4 after 20 iterations.  Integer outputs
+(kernel-call and pixel counters) must be identical.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from jpet_strip import capi, phantom
+
+pytestmark = pytest.mark.gpu
+
+TOL_ITER = 1e-5
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+
+def _geoms(c):
+    g = c["geometry"]
+    args = (g["R"], g["L"], g["n_y"], g["n_z"], g["p"], g["sz"], g["sdl"])
+    return capi.Geometry(*args), O.Geometry(*args)
+
+
+@pytest.mark.parametrize("case", ["c1", "crop"])
+def test_iterations_match_reference_goldens(golden, case):
+    manifest, load = golden
+    c = manifest[case]
+    cg, _ = _geoms(c)
+    ev = load(f"{case}_events.npy")
+    with capi.StripReconstruction(cg) as rec:
+        rec.set_events(ev)
+        done = 0
+        for it in c["iterations"]:
+            rec.iterate(it - done)
+            done = it
+            got = rec.rho
+            want = load(f"{case}_strict_it{it:02d}.npy")
+            assert rel_l2(got, want) < TOL_ITER, (case, it, rel_l2(got, want))
+        want = load(f"{case}_release_it{done:02d}.npy")
+        assert rel_l2(got, want) < TOL_ITER
+
+
+@pytest.mark.parametrize("case", ["c1", "crop"])
+def test_each_iteration_and_counters_match_oracle(golden, case):
+    manifest, load = golden
+    c = manifest[case]
+    cg, og = _geoms(c)
+    ev = load(f"{case}_events.npy")
+    with capi.StripReconstruction(cg) as rec:
+        rec.set_events(ev)
+        rho = None
+        for it in range(3):
+            rec.iterate(1)
+            rho, st = O.mlem_f(og, ev, 1, rho, threads=4)
+            got = rec.rho
+            assert rel_l2(got, rho) < TOL_ITER, (it, rel_l2(got, rho))
+            cnt = rec.counters()
+            assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
+            assert cnt["n_pixels"] == st["n_pixels"]
+            assert cnt["n_contributing"] == st["n_contributing"]
+            rec.rho = rho  # continue both from the same image
+
+
+def test_twenty_iterations_stay_within_1e4(golden):
+    manifest, load = golden
+    cg, og = _geoms(manifest["c1"])
+    ev = load("c1_events.npy")
+    with capi.StripReconstruction(cg) as rec:
+        rec.set_events(ev)
+        rec.iterate(20)
+        got = rec.rho
+    want, _ = O.mlem_f(og, ev, 20, threads=8)
+    assert rel_l2(got, want) < 1e-4
+
+
+def test_mass_conservation_and_nonnegativity(golden):
+    manifest, load = golden
+    cg, _ = _geoms(manifest["c1"])
+    ev = load("c1_events.npy")
+    with capi.StripReconstruction(cg) as rec:
+        rec.set_events(ev)
+        rec.iterate(2)
+        r = rec.rho
+        cnt = rec.counters()
+    assert (r >= 0).all()
+    assert abs(r.astype(np.float64).sum() - cnt["n_contributing"]) < 1e-6 * len(ev) + 1e-2
+
+
+def test_initial_image_and_set_image_roundtrip():
+    g = capi.Geometry(450, 1000, 90, 100, 10, 10, 42)
+    with capi.StripReconstruction(g) as rec:
+        assert np.array_equal(rec.rho, np.ones((90, 100), np.float32))
+        x = np.random.default_rng(0).random((90, 100)).astype(np.float32)
+        rec.rho = x
+        assert np.array_equal(rec.rho, x)
+
+
+def test_empty_event_list_and_iterate_before_events():
+    g = capi.Geometry(450, 1000, 90, 100, 10, 10, 42)
+    with capi.StripReconstruction(g) as rec:
+        with pytest.raises(capi.StripError) as e:
+            rec.iterate(1)
+        assert e.value.code == capi.JPET_ERR_STATE
+        rec.set_events(np.zeros((0, 3), np.float32))
+        rec.iterate(1)
+        assert not rec.rho.any()
+
+
+def test_edge_events_outside_grid_nan_and_single(golden):
+    # events far outside, on the grid corner, NaN and Inf: same result as the oracle
+    og = O.Geometry(450, 1000, 90, 100, 5, 10, 42)
+    cg = capi.Geometry(450, 1000, 90, 100, 5, 10, 42)
+    ev = np.array([
+        [0.0, 0.0, 0.0],            # centre
+        [240.0, 260.0, 200.0],      # near the grid corner
+        [900.0, 900.0, 0.0],        # far outside in z
+        [0.0, 0.0, 2000.0],         # far outside in y
+        [np.nan, 0.0, 0.0],
+        [np.inf, -np.inf, 0.0],
+        [1e30, -1e30, 1e30],
+        [-249.0, -251.0, -170.0],
+    ], np.float32)
+    for sl in (slice(0, 1), slice(None)):
+        with capi.StripReconstruction(cg) as rec:
+            rec.set_events(ev[sl])
+            rec.iterate(1)
+            got = rec.rho
+            cnt = rec.counters()
+        want, st = O.mlem_f(og, ev[sl], 1, threads=1)
+        assert np.isfinite(got).all()
+        assert rel_l2(got, want) < TOL_ITER
+        assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
+
+
+def test_zero_image_gives_zero_without_nan(golden):
+    manifest, load = golden
+    cg, og = _geoms(manifest["c1"])
+    ev = load("c1_events.npy")[:500]
+    with capi.StripReconstruction(cg) as rec:
+        rec.set_events(ev)
+        rec.rho = np.zeros((cg.n_y, cg.n_z), np.float32)
+        rec.iterate(1)
+        got = rec.rho
+        assert rec.counters()["n_contributing"] == 0
+    assert not got.any()
+
+
+def test_sensitivity_maps_match_oracle():
+    for g in [(450, 1000, 180, 200, 5, 10, 42), (500, 200, 64, 40, 5, 10, 63)]:
+        cg, og = capi.Geometry(*g), O.Geometry(*g)
+        with capi.StripReconstruction(cg) as rec:
+            for kind in (0, 1):
+                got = rec.sensitivity(kind)
+                want = O.sensitivity_map(og, kind)
+                np.testing.assert_allclose(got, want, rtol=2e-6, atol=1e-7)
+
+
+def test_gpu_reference_semantics_mode(golden):
+    manifest, load = golden
+    cg, og = _geoms(manifest["c1"])
+    ev = load("c1_events.npy")
+    with capi.StripReconstruction(cg, mode=capi.MODE_GPU_REFERENCE) as rec:
+        rec.set_events(ev)
+        rec.iterate(2)
+        got = rec.rho
+    want = O.mlem_gpuref(og, ev, 2, threads=4)
+    assert rel_l2(got, want) < TOL_ITER
+
+
+def test_run_callback_protocol(golden):
+    manifest, load = golden
+    cg, og = _geoms(manifest["c1"])
+    ev = load("c1_events.npy")[:3000]
+    rho = np.ones((cg.n_y, cg.n_z), np.float32)
+    outputs, progress = [], []
+    name = capi.run(cg, ev, rho, 2, 3, output=lambda it, img: outputs.append((it, img)),
+                    progress=lambda done, fin: progress.append((done, fin)))
+    assert name
+    # output(-1, sensitivity), then i+1 for i < I-1 in block 0, then block ends
+    assert [o[0] for o in outputs] == [-1, 1, 2, 3, 6]
+    assert progress[:2] == [(0, False), (0, True)] and progress[-1] == (6, False)
+    want, _ = O.mlem_f(og, ev, 6, threads=4)
+    assert rel_l2(rho, want) < 1e-5
+    assert rel_l2(outputs[-1][1], want) < 1e-5
+    np.testing.assert_allclose(outputs[0][1], O.sensitivity_map(og, 1), rtol=2e-6)
+
+
+def test_forced_small_windows_exercise_large_box_path(golden):
+    # a 1x1 tile with the default window budget still covers every event; a
+    # tiny tile request keeps results identical regardless of the tiling
+    manifest, load = golden
+    cg, og = _geoms(manifest["c1"])
+    ev = load("c1_events.npy")
+    want, st = O.mlem_f(og, ev, 1, threads=4)
+    for tw, th in [(1, 1), (8, 32), (64, 16)]:
+        with capi.StripReconstruction(cg, tile_w=tw, tile_h=th) as rec:
+            rec.set_events(ev)
+            rec.iterate(1)
+            assert rel_l2(rec.rho, want) < TOL_ITER
+            assert rec.counters()["n_kernel_calls"] == st["n_kernel_calls"]
+
+
+def test_larger_random_phantom_against_oracle():
+    # 2 mm grid, 10-ellipse phantom, 30k events
+    ell = phantom.random_ellipse_phantom(seed=7)
+    ev = phantom.generate_events(ell, 30000, 450.0, 1000.0, 10.0, 42.0, seed=7)
+    args = (450.0, 1000.0, 450, 500, 2.0, 10.0, 42.0)
+    cg, og = capi.Geometry(*args), O.Geometry(*args)
+    with capi.StripReconstruction(cg) as rec:
+        rec.set_events(ev)
+        rho = None
+        for _ in range(2):
+            rec.iterate(1)
+            rho, st = O.mlem_f(og, ev, 1, rho, threads=8)
+            assert rel_l2(rec.rho, rho) < TOL_ITER
+            rec.rho = rho
+        assert rec.counters()["n_kernel_calls"] == st["n_kernel_calls"]
