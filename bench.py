@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-peaks", action="store_true", help="skip the peak microbenchmarks")
+    p.add_argument("--variant", type=int, default=0, help="0 fast kernel, 1 exact kernel")
     return p.parse_args()
 
 
@@ -116,12 +118,14 @@ class ClockSampler:
 
 def measured_peaks(device: int):
     lib = C.CDLL(os.path.join(PKG, "lib", "libjpet_peaks.so"))
-    out = (C.c_double * 6)()
+    out = (C.c_double * 9)()
     rc = lib.jpet_peaks_measure(device, out)
     if rc != 0:
         raise RuntimeError(f"peak microbenchmark failed: {rc}")
     return {"ex2_per_s": out[0], "ffma_per_s": out[1], "shared_atomic_per_s": out[2],
-            "global_atomic_per_s": out[3], "sms": int(out[4]), "sm_clock_khz": int(out[5])}
+            "global_atomic_per_s": out[3], "sms": int(out[4]), "sm_clock_khz": int(out[5]),
+            "shared_atomic_u32_per_s": out[6], "shared_atomic_u64_per_s": out[7],
+            "shared_rmw_per_s": out[8]}
 
 
 def hbm_peak():
@@ -207,9 +211,9 @@ def gb300_arm(args, wl, world, rank, local):
     n_events = args.events or wl.n_events
     events = wl.events(n_events)
     geom = capi.Geometry(*wl.geometry_args())
-    peaks = measured_peaks(local)
+    peaks = None if args.no_peaks else measured_peaks(local)
     stream = torch.cuda.Stream()
-    rec = capi.StripReconstruction(geom, device=local)
+    rec = capi.StripReconstruction(geom, device=local, variant=args.variant)
     rec.set_stream(stream.cuda_stream)
     rec.set_events(events)
     with torch.cuda.stream(stream):
@@ -294,8 +298,23 @@ def gb300_arm(args, wl, world, rank, local):
     if rank != 0:
         return
     hbm, hbm_kind = hbm_peak()
-    ex2_peak = peaks["ex2_per_s"]
-    atom_frac = evals_per_s / peaks["shared_atomic_per_s"]
+    roofline = None
+    if peaks:
+        ex2_peak = peaks["ex2_per_s"]
+        atom_peak = peaks["shared_atomic_per_s"]
+        # one exp and one shared-memory atomic per kernel-pixel evaluation: the
+        # lower of the two peaks binds
+        bound_sfu = ex2_peak <= atom_peak
+        peak = ex2_peak if bound_sfu else atom_peak
+        roofline = {"bound": "sfu" if bound_sfu else "shared_atomic",
+                    "achieved": evals_per_s / 1e9, "peak": peak / 1e9,
+                    "unit": "Gex2/s" if bound_sfu else "Gatomic/s",
+                    "frac": evals_per_s / peak,
+                    "peak_source": "measured on this GPU by libjpet_peaks (ex2.approx and "
+                                   "shared float atomicAdd throughput)",
+                    "sfu_frac": evals_per_s / ex2_peak,
+                    "shared_atomic_frac": evals_per_s / atom_peak,
+                    "traffic": None, "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_kind}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -307,11 +326,7 @@ def gb300_arm(args, wl, world, rank, local):
                    "parallelism": f"replicas{world}"},
         "kernel_pixel_evals_per_s": world * evals_per_s,
         "evals_per_event": evals_per_iter / n_events,
-        "roofline": {"bound": "sfu", "achieved": evals_per_s / 1e9, "peak": ex2_peak / 1e9,
-                     "unit": "Gex2/s", "frac": evals_per_s / ex2_peak,
-                     "peak_source": "measured ex2.approx rate on this GPU (libjpet_peaks)",
-                     "shared_atomic_frac": atom_frac,
-                     "traffic": None, "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_kind},
+        "roofline": roofline,
         "accuracy": accuracy,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT,

@@ -66,6 +66,10 @@ typedef struct jpet_strip_geom {
 #define JPET_PRECISION_KAHAN 1      /* FP32 evaluation, compensated per-tile sums */
 #define JPET_PRECISION_FP64_DEN 2   /* as KAHAN, plus per-event denominators reduced in FP64 */
 
+/* iteration kernel */
+#define JPET_VARIANT_FAST 0  /* exp2-form kernel, packed f32x2, register-cached K*rho (default) */
+#define JPET_VARIANT_EXACT 1 /* every pixel evaluated in the reference's operation order */
+
 typedef struct jpet_strip_opts {
   int32_t device;       /* CUDA device ordinal (-D / --cuda-device) */
   int32_t mode;         /* JPET_MODE_* */
@@ -73,7 +77,8 @@ typedef struct jpet_strip_opts {
   int32_t tile_w;       /* image tile width in pixels, 0 = chosen by the tuner */
   int32_t tile_h;       /* image tile height in pixels, 0 = chosen by the tuner */
   int32_t block_threads;/* threads per CTA of the iteration kernel, 0 = tuned */
-  int32_t reserved[10]; /* must be zero */
+  int32_t variant;      /* JPET_VARIANT_*; the GPU-reference mode always runs EXACT */
+  int32_t reserved[9];  /* must be zero */
 } jpet_strip_opts;
 
 /* Per-iteration counters (the reference's ReconstructionStats,

@@ -63,12 +63,59 @@ __global__ void atoms_kernel(float* out, int iters) {
   __shared__ float sm[1024];
   sm[threadIdx.x] = 0.0f;
   __syncthreads();
-  float* p = &sm[threadIdx.x];
+  // four independent words per thread, each warp instruction conflict-free
+  float* p = &sm[threadIdx.x & 255];
   for (int i = 0; i < iters; ++i) {
     atomicAdd(p, 1.0f);
-    atomicAdd(p, 1.0f);
-    atomicAdd(p, 1.0f);
-    atomicAdd(p, 1.0f);
+    atomicAdd(p + 256, 1.0f);
+    atomicAdd(p + 512, 1.0f);
+    atomicAdd(p + 768, 1.0f);
+  }
+  __syncthreads();
+  if (sm[threadIdx.x] == -1.0f) out[threadIdx.x] = sm[threadIdx.x];
+}
+
+__global__ void atoms_u32_kernel(unsigned* out, int iters) {
+  __shared__ unsigned sm[1024];
+  sm[threadIdx.x] = 0u;
+  __syncthreads();
+  unsigned* p = &sm[threadIdx.x & 255];
+  for (int i = 0; i < iters; ++i) {
+    atomicAdd(p, 3u);
+    atomicAdd(p + 256, 3u);
+    atomicAdd(p + 512, 3u);
+    atomicAdd(p + 768, 3u);
+  }
+  __syncthreads();
+  if (sm[threadIdx.x] == 1u) out[threadIdx.x] = sm[threadIdx.x];
+}
+
+__global__ void atoms_u64_kernel(unsigned long long* out, int iters) {
+  __shared__ unsigned long long sm[512];
+  if (threadIdx.x < 512) sm[threadIdx.x] = 0ull;
+  __syncthreads();
+  unsigned long long* p = &sm[threadIdx.x & 127];
+  for (int i = 0; i < iters; ++i) {
+    atomicAdd(p, 3ull);
+    atomicAdd(p + 128, 3ull);
+    atomicAdd(p + 256, 3ull);
+    atomicAdd(p + 384, 3ull);
+  }
+  __syncthreads();
+  if (threadIdx.x < 512 && sm[threadIdx.x] == 1ull) out[threadIdx.x] = sm[threadIdx.x];
+}
+
+// plain read-modify-write of a private shared word (LDS + FADD + STS)
+__global__ void rmw_kernel(float* out, int iters) {
+  __shared__ float sm[1024];
+  sm[threadIdx.x] = 0.0f;
+  __syncthreads();
+  volatile float* p = &sm[threadIdx.x & 255];
+  for (int i = 0; i < iters; ++i) {
+    p[0] = p[0] + 1.0f;
+    p[256] = p[256] + 1.0f;
+    p[512] = p[512] + 1.0f;
+    p[768] = p[768] + 1.0f;
   }
   __syncthreads();
   if (sm[threadIdx.x] == -1.0f) out[threadIdx.x] = sm[threadIdx.x];
@@ -106,9 +153,10 @@ double best_rate(F launch, double ops, int reps) {
 
 extern "C" {
 
-// out[0] ex2/s, out[1] ffma/s, out[2] shared atomics/s, out[3] global atomics/s,
-// out[4] number of SMs, out[5] SM clock (kHz, device attribute).  Returns 0 or
-// a CUDA error code.
+// out[0] ex2/s, out[1] ffma/s, out[2] shared float atomics/s, out[3] global
+// float atomics/s, out[4] number of SMs, out[5] SM clock (kHz, device
+// attribute), out[6] shared u32 atomics/s, out[7] shared u64 atomics/s,
+// out[8] plain shared read-modify-writes/s.  Returns 0 or a CUDA error code.
 int jpet_peaks_measure(int device, double* out) {
   if (cudaSetDevice(device) != cudaSuccess) return 1;
   int sms = 0, clk = 0;
@@ -130,6 +178,14 @@ int jpet_peaks_measure(int device, double* out) {
                      double(blocks) * threads * it_red, 5);
   out[4] = sms;
   out[5] = clk;
+  out[6] = best_rate([&] { atoms_u32_kernel<<<blocks, threads>>>(reinterpret_cast<unsigned*>(buf),
+                                                                 it_ats); },
+                     double(blocks) * threads * it_ats * 4, 5);
+  out[7] = best_rate([&] { atoms_u64_kernel<<<blocks, threads>>>(
+                               reinterpret_cast<unsigned long long*>(buf), it_ats); },
+                     double(blocks) * threads * it_ats * 4, 5);
+  out[8] = best_rate([&] { rmw_kernel<<<blocks, threads>>>(buf, it_ats); },
+                     double(blocks) * threads * it_ats * 4, 5);
   cudaError_t e = cudaDeviceSynchronize();
   cudaFree(buf);
   return e == cudaSuccess ? 0 : static_cast<int>(e);

@@ -66,6 +66,11 @@ struct jpet_strip {
   DevBuf<short4> ev_box, sorted_box, over_box;
   DevBuf<int32_t> ev_key, tile_count, tile_offset, tile_cursor, hist, small;
   DevBuf<Chunk> chunks;
+  DevBuf<uint16_t> row_table;
+  FastConst fc{};
+  bool use_fast = false;
+  bool counters_valid = false;
+  unsigned long long table_kernel_calls = 0;
   DevBuf<unsigned long long> box_pixels;
   DevBuf<DevCounters> counters;
 
@@ -176,8 +181,8 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
     }
     return 1;
   };
-  int mw = std::max(1, pct(hw, 0.99999));
-  int mh = std::max(1, pct(hh, 0.99999));
+  int mw = std::min(255, std::max(1, pct(hw, 0.99999)));
+  int mh = std::min(1024, std::max(1, pct(hh, 0.99999)));
   // shrink the box limits until at least an 8x8 tile fits
   while ((mw + 8) * (mh + 8) > budget_px) {
     if (mw >= mh) mw = mw * 7 / 8; else mh = mh * 7 / 8;
@@ -205,6 +210,18 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
   t.chunk_events = 512;
   t.threads = o.block_threads > 0 ? o.block_threads : 256;
   t.group = 32;
+  t.row_stride = (mh + 1) & ~1;
+  // register-cache shape of the fast kernel from the rows of 99.9% of the boxes
+  // (fast_width_shape adds the widest in-ellipse row)
+  const int rows999 = pct(hh, 0.999);
+  t.fast_shape = rows999 <= 32 ? kShapeS : (rows999 <= 64 ? kShapeM : kShapeL);
+}
+
+// The widest in-ellipse row is 2 * 3 sigma_z / sqrt(2) / pixel (+ rounding).
+int fast_width_shape(const DevGeom& g) {
+  const double half = 3.0 * g.sigma_z / std::sqrt(2.0) / g.pixel_width;
+  const int w = 2 * static_cast<int>(half) + 3;
+  return w <= 16 ? kShapeS : (w <= 24 ? kShapeM : kShapeL);
 }
 
 int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const float* d_dl,
@@ -242,6 +259,7 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
   int64_t nonempty = 0;
   for (int b = 1; b < kHistBins; ++b) nonempty += hw[b];
   choose_tiling(h->opts, hw, hh, nonempty, h->g.n_y, h->g.n_z, h->tiling);
+  h->tiling.fast_shape = std::max(h->tiling.fast_shape, fast_width_shape(h->g));
   const Tiling& t = h->tiling;
   const int32_t n_tiles = t.n_tiles_x * t.n_tiles_y;
   JPET_CUDA(h, h->tile_count.alloc(n_tiles), "cudaMalloc(tiles)");
@@ -295,12 +313,26 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
                                      h->tile_cursor.p, h->sorted_geom.p, h->sorted_box.p,
                                      h->small.p + 1, h->over_geom.p, h->over_box.p, s),
             "scatter_events launch");
+  h->use_fast = h->opts.mode == JPET_MODE_CPU_REFERENCE && h->opts.variant == JPET_VARIANT_FAST;
+  h->table_kernel_calls = 0;
+  if (h->use_fast && acc > 0) {
+    JPET_CUDA(h, h->row_table.alloc(static_cast<size_t>(acc) * t.row_stride),
+              "cudaMalloc(row table)");
+    JPET_CUDA(h, cudaMemsetAsync(h->box_pixels.p, 0, sizeof(unsigned long long), s), "memset");
+    JPET_CUDA(h, launch_row_tables(h->g, t, acc, h->sorted_geom.p, h->sorted_box.p,
+                                   h->row_table.p, h->box_pixels.p, s),
+              "row_table launch");
+    JPET_CUDA(h, cudaMemcpyAsync(&h->table_kernel_calls, h->box_pixels.p,
+                                 sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
+              "copy counter");
+  }
   JPET_CUDA(h, cudaStreamSynchronize(s), "scatter_events");
   // unsorted copies are no longer needed
   h->ev_geom.release();
   h->ev_box.release();
   h->ev_key.release();
   h->events_ready = true;
+  h->counters_valid = false;
   return JPET_OK;
 }
 
@@ -365,6 +397,10 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
     g_create_error = "unknown mode";
     return JPET_ERR_ARGUMENT;
   }
+  if (o.variant != JPET_VARIANT_FAST && o.variant != JPET_VARIANT_EXACT) {
+    g_create_error = "unknown kernel variant";
+    return JPET_ERR_ARGUMENT;
+  }
   if (o.precision != JPET_PRECISION_FP32) {
     g_create_error = "precision mode not available in this build";
     return JPET_ERR_UNSUPPORTED;
@@ -393,6 +429,9 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
   h->opts = o;
   h->device = o.device;
   h->g = make_geom(*geom);
+  h->fc.kz = -1.4426950408889634f * h->g.ipz;
+  h->fc.kdl = -2.0f * 1.4426950408889634f * h->g.ipd;
+  h->fc.two_r2 = 2.0f * h->g.radius * h->g.radius;
   e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
@@ -444,6 +483,7 @@ int jpet_strip_destroy(jpet_strip_t* h) {
   h->hist.release();
   h->small.release();
   h->chunks.release();
+  h->row_table.release();
   h->box_pixels.release();
   h->counters.release();
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -518,15 +558,23 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
   for (int it = 0; it < n; ++it) {
     JPET_CUDA(h, cudaMemsetAsync(h->out.p, 0, n_pix * sizeof(float), s), "clear image");
     JPET_CUDA(h, cudaMemsetAsync(h->counters.p, 0, sizeof(DevCounters), s), "clear counters");
-    JPET_CUDA(h, launch_iterate(h->g, h->tiling, h->opts.mode, h->chunks.p, h->n_chunks,
-                                h->sorted_geom.p, h->sorted_box.p, h->rho.p, sens, h->out.p,
-                                h->counters.p, s),
-              "iteration kernel launch");
+    if (h->use_fast) {
+      JPET_CUDA(h, launch_iterate_fast(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
+                                       h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
+                                       h->rho.p, h->out.p, h->counters.p, s),
+                "iteration kernel launch");
+    } else {
+      JPET_CUDA(h, launch_iterate(h->g, h->tiling, h->opts.mode, h->chunks.p, h->n_chunks,
+                                  h->sorted_geom.p, h->sorted_box.p, h->rho.p, sens, h->out.p,
+                                  h->counters.p, s),
+                "iteration kernel launch");
+    }
     JPET_CUDA(h, launch_iterate_global(h->g, h->opts.mode, h->n_oversize, h->over_geom.p,
                                        h->over_box.p, h->rho.p, sens, h->out.p, h->counters.p, s),
               "large-box kernel launch");
     std::swap(h->rho, h->out);
     ++h->iterations_done;
+    h->counters_valid = true;
   }
   return JPET_OK;
 }
@@ -569,7 +617,9 @@ int jpet_strip_get_counters(jpet_strip_t* h, jpet_strip_counters* out) {
   std::memset(out, 0, sizeof(*out));
   out->n_events = h->n_events;
   out->n_pixels = static_cast<int64_t>(h->total_box_pixels);
-  out->n_kernel_calls = static_cast<int64_t>(c.n_kernel_calls);
+  out->n_kernel_calls = static_cast<int64_t>(c.n_kernel_calls) +
+                        (h->use_fast && h->counters_valid
+                             ? static_cast<int64_t>(h->table_kernel_calls) : 0);
   out->n_contributing = static_cast<int64_t>(c.n_contributing);
   out->n_oversize = h->n_oversize;
   out->n_tiles = h->n_tiles_nonempty;

@@ -1,0 +1,321 @@
+// Fast sm_103a MLEM iteration for the CPU-reference semantics.
+//
+// Two pieces:
+//
+// 1. row_table_kernel (once per event set): for every sorted event and every
+//    row of its clamped box, the exact column interval whose pixel centres pass
+//    the reference's 3-sigma test (GaussianKernel::in_ellipse,
+//    src/2d/strip/gaussian_kernel.h:131-137, evaluated in the reference's
+//    rounding).  The test's quadratic form is convex along a row, so the passing
+//    columns are one interval; it is found from the analytic endpoints
+//    tan*dy +- sqrt((9 - 4 ipd sec^2 dy^2) / (2 ipz)) and corrected by evaluating
+//    the exact test around them.  Stored as 16 bits per row: first column
+//    relative to the box (8 bits) and width (8 bits).  The pixel set of every
+//    event is therefore exactly the reference's, without any per-pixel test in
+//    the iterations.
+//
+// 2. iterate_fast_kernel (every iteration): one CTA per chunk of events of one
+//    image tile, rho window and back-projection window in shared memory (as the
+//    exact kernel).  One warp per event; 4 lanes per image row, 8 rows per step,
+//    each lane two adjacent pixels per 8-column sweep, so that the packed f32x2
+//    instructions of sm_100+ (FFMA2/FADD2/FMUL2) evaluate two pixels each.  The
+//    kernel value is rewritten so that a pixel costs one exp2:
+//
+//      K = c0 / sqrt(aMa) * exp(-bMb / 2)                      (gaussian_kernel.h:51-79)
+//      bMb = 2 ipz u^2 + 4 ipd sec^2 dy^2,  u = dz - dy tan,  dy = py - y
+//      aMa = 2 ipz sec^4 (py^2 + R^2) + 4 ipd sec^2 tan^2 py^2
+//      K / K_ref = 2^(kz u^2 + ky dy^2 - log2(aMa(py)/aMa(y)) / 2)
+//
+//    with kz = -log2(e) ipz and ky = -2 log2(e) ipd sec^2; K_ref = c0/sqrt(aMa(y))
+//    is a per-event constant that cancels in K rho / sum K rho.  Along a row,
+//    u = u0 + j pw for the j-th in-ellipse pixel, so the exponent is
+//    P_row + Q_row j + kz pw^2 j^2 with a per-lane constant for the last term.
+//    The exponent is evaluated with ex2.approx, the row prefactor with
+//    lg2.approx.  K rho of every pixel stays in registers between the forward
+//    sum and the back-projection (shared-memory atomics).  Events whose box does
+//    not fit the register cache take the exact warp rasteriser instead.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "strip_device.cuh"
+#include "strip_internal.h"
+#include "strip_raster.cuh"
+
+namespace jpet {
+namespace {
+
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// ---------------------------------------------------------------------------------
+// exact per-row intervals
+// ---------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) row_table_kernel(DevGeom g, int32_t n, int32_t stride,
+                                                        const float4* __restrict__ ev_geom,
+                                                        const short4* __restrict__ ev_box,
+                                                        uint16_t* __restrict__ rows,
+                                                        unsigned long long* kernel_calls) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_warps = (gridDim.x * blockDim.x) >> 5;
+  unsigned long long calls = 0;
+  for (int e = warp; e < n; e += n_warps) {
+    const float4 ev = ev_geom[e];
+    const short4 b = ev_box[e];
+    const float z = ev.x, y = ev.y, t = ev.z, sec = ev.w;
+    float A, B, C;
+    ellipse_abc(g, t, sec, A, B, C);
+    const float sec2_ipd4 = 4.0f * sec * sec * g.ipd;
+    const float inv_2ipz = 0.5f / g.ipz;
+    const float inv_pw = 1.0f / g.pixel_width;
+    const int nrows = b.w - b.y;
+    const int bx = b.x, bz = b.z;
+    for (int ri = lane; ri < nrows; ri += 32) {
+      const int iy = b.y + ri;
+      const float dy = __fsub_rn(pixel_center_y(g, iy), y);
+      auto pass = [&](int c) { return in_ellipse(A, B, C, dy, __fsub_rn(pixel_center_z(g, c), z)); };
+      const float h = sqrtf(fmaxf((9.0f - sec2_ipd4 * dy * dy) * inv_2ipz, 0.0f)) * inv_pw;
+      const float xc = (z + t * dy - g.tl_z_half_w) * inv_pw;
+      const float fbx = static_cast<float>(bx), fbz = static_cast<float>(bz - 1);
+      // the column nearest the minimum of the convex test quadratic
+      int cs = static_cast<int>(fminf(fmaxf(rintf(xc), fbx), fbz));
+      bool any = pass(cs);
+      if (!any && cs - 1 >= bx && pass(cs - 1)) {
+        cs -= 1;
+        any = true;
+      }
+      if (!any && cs + 1 < bz && pass(cs + 1)) {
+        cs += 1;
+        any = true;
+      }
+      int w = 0, first = bx;
+      if (any) {
+        int lo = static_cast<int>(fminf(fmaxf(ceilf(xc - h), fbx), static_cast<float>(cs)));
+        if (pass(lo)) {
+          while (lo > bx && pass(lo - 1)) --lo;
+        } else {
+          while (lo < cs && !pass(lo)) ++lo;
+        }
+        int hi = static_cast<int>(fminf(fmaxf(floorf(xc + h), static_cast<float>(cs)), fbz));
+        if (pass(hi)) {
+          while (hi < bz - 1 && pass(hi + 1)) ++hi;
+        } else {
+          while (hi > cs && !pass(hi)) --hi;
+        }
+        first = lo;
+        w = hi - lo + 1;
+      }
+      rows[static_cast<size_t>(e) * stride + ri] =
+          static_cast<uint16_t>((first - bx) | (w << 8));
+      calls += static_cast<unsigned long long>(w);
+    }
+  }
+  calls = warp_sum_u64(calls);
+  if (lane == 0 && calls) atomicAdd(kernel_calls, calls);
+}
+
+// ---------------------------------------------------------------------------------
+// fast iteration
+// ---------------------------------------------------------------------------------
+
+constexpr int kG = 4;          // lanes per image row
+constexpr int kRPS = 32 / kG;  // rows per step
+constexpr int kCols = 2 * kG;  // columns per sweep
+
+template <int RS, int SW>
+__global__ void __launch_bounds__(256) iterate_fast_kernel(
+    DevGeom g, FastConst fc, Tiling t, const Chunk* __restrict__ chunks,
+    const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
+    const uint16_t* __restrict__ rows, const float* __restrict__ rho, float* __restrict__ out,
+    DevCounters* counters) {
+  extern __shared__ float smem[];
+  const int pitch = t.win_w;
+  const int win = t.win_w * t.win_h;
+  float* w_rho = smem;
+  float* w_out = smem + win;
+  const Chunk c = chunks[blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+  for (int r = warp; r < t.win_h; r += n_warps) {
+    const int gy = c.oy + r;
+    for (int col = lane; col < t.win_w; col += 32) {
+      const int gx = c.ox + col;
+      w_rho[r * pitch + col] = (gy < g.n_y && gx < g.n_z) ? rho[gy * g.n_z + gx] : 0.0f;
+      w_out[r * pitch + col] = 0.0f;
+    }
+  }
+  __syncthreads();
+
+  const int gid = lane / kG;  // row of the step this lane works on
+  const int gl = lane % kG;   // lane within the row group
+  // per-lane sweep constants: pixel offsets j, j+1 and kz pw^2 j^2
+  float2 jf[SW], cj[SW];
+  const float kzp2 = fc.kz * g.pixel_width * g.pixel_width;
+#pragma unroll
+  for (int s = 0; s < SW; ++s) {
+    const float j0 = static_cast<float>(2 * gl + kCols * s);
+    jf[s] = make_float2(j0, j0 + 1.0f);
+    cj[s] = make_float2(kzp2 * j0 * j0, kzp2 * (j0 + 1.0f) * (j0 + 1.0f));
+  }
+  constexpr int kEntRegs = (RS * kRPS + 31) / 32;
+
+  WindowAccess acc{w_rho, w_out, c.ox, c.oy, pitch};
+  unsigned long long contrib = 0, dummy_calls = 0;
+  for (int e = warp; e < c.count; e += n_warps) {
+    const int ei = c.start + e;
+    const float4 ev = ev_geom[ei];
+    const short4 box = ev_box[ei];
+    const int nrows = box.w - box.y;
+    const uint16_t* rt = rows + static_cast<size_t>(ei) * t.row_stride;
+    // the event's row table in registers: lane l holds rows l, l+32, l+64
+    uint32_t ent[kEntRegs];
+    int maxw = 0;
+#pragma unroll
+    for (int k = 0; k < kEntRegs; ++k) {
+      const int ri = lane + 32 * k;
+      ent[k] = (ri < nrows) ? rt[ri] : 0u;
+      maxw = max(maxw, static_cast<int>(ent[k] >> 8));
+    }
+    maxw = __reduce_max_sync(kFull, maxw);
+    if (nrows > RS * kRPS || maxw > SW * kCols) {
+      process_event<kCpuReference>(g, 32, ev, box, acc, nullptr, dummy_calls, contrib);
+      continue;
+    }
+    const float z = ev.x, y = ev.y, tn = ev.z, sec = ev.w;
+    const float sec2 = sec * sec;
+    const float ky = fc.kdl * sec2;
+    // aMa(py) = P + Q py^2
+    const float P = fc.two_r2 * sec2 * sec2 * g.ipz;
+    const float Q = 2.0f * sec2 * sec2 * g.ipz + 4.0f * sec2 * tn * tn * g.ipd;
+    const float lref = 0.5f * lg2_approx(fmaf(Q, y * y, P));
+    const float u_base = g.tl_z_half_w - z;
+    const int n_steps = (nrows + kRPS - 1) / kRPS;
+
+    float2 cache[RS][SW];
+    float2 den2 = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int rs = 0; rs < RS; ++rs) {
+      if (rs < n_steps) {
+        const int ri = rs * kRPS + gid;
+        const uint32_t en = __shfl_sync(kFull, ent[(rs * kRPS) / 32], (rs * kRPS) % 32 + gid);
+        const int w = (ri < nrows) ? static_cast<int>(en >> 8) : 0;
+        const int c_lo = box.x + static_cast<int>(en & 255u);
+        const int iy = box.y + ri;
+        const float py = g.tl_y_half_h - static_cast<float>(iy) * g.pixel_height;
+        const float dy = py - y;
+        const float lf = lref - 0.5f * lg2_approx(fmaf(Q, py * py, P));
+        const float u0 = fmaf(static_cast<float>(c_lo), g.pixel_width, u_base - dy * tn);
+        const float p_row = fmaf(fc.kz * u0, u0, fmaf(ky * dy, dy, lf));
+        const float q_row = 2.0f * fc.kz * g.pixel_width * u0;
+        const float* rp = w_rho + (iy - c.oy) * pitch + (c_lo - c.ox);
+#pragma unroll
+        for (int s = 0; s < SW; ++s) {
+          const int j = 2 * gl + kCols * s;
+          float2 kr = make_float2(0.0f, 0.0f);
+          if (j < w) {
+            const float2 a = __ffma2_rn(make_float2(q_row, q_row), jf[s],
+                                        __fadd2_rn(make_float2(p_row, p_row), cj[s]));
+            const float2 ex = make_float2(ex2_approx(a.x), ex2_approx(a.y));
+            const float2 r2 = make_float2(rp[j], rp[j + 1]);
+            kr = __fmul2_rn(ex, r2);
+            if (j + 1 >= w) kr.y = 0.0f;
+          }
+          cache[rs][s] = kr;
+          den2 = __fadd2_rn(den2, kr);
+        }
+      }
+    }
+    const float den = warp_sum(den2.x + den2.y);
+    if (!(den > 0.0f)) continue;  // inv_denominator = 0 (reconstruction.h:290)
+    if (lane == 0) ++contrib;
+    const float inv = __fdiv_rn(1.0f, den);
+    const float2 inv2 = make_float2(inv, inv);
+#pragma unroll
+    for (int rs = 0; rs < RS; ++rs) {
+      if (rs < n_steps) {
+        const int ri = rs * kRPS + gid;
+        const uint32_t en = __shfl_sync(kFull, ent[(rs * kRPS) / 32], (rs * kRPS) % 32 + gid);
+        const int w = (ri < nrows) ? static_cast<int>(en >> 8) : 0;
+        const int c_lo = box.x + static_cast<int>(en & 255u);
+        float* op = w_out + (box.y + ri - c.oy) * pitch + (c_lo - c.ox);
+#pragma unroll
+        for (int s = 0; s < SW; ++s) {
+          const int j = 2 * gl + kCols * s;
+          if (j < w) {
+            const float2 v = __fmul2_rn(cache[rs][s], inv2);
+            atomicAdd(op + j, v.x);
+            if (j + 1 < w) atomicAdd(op + j + 1, v.y);
+          }
+        }
+      }
+    }
+  }
+  if (lane == 0 && contrib) atomicAdd(&counters->n_contributing, contrib);
+  __syncthreads();
+  for (int r = warp; r < t.win_h; r += n_warps) {
+    const int gy = c.oy + r;
+    for (int col = lane; col < t.win_w; col += 32) {
+      const int gx = c.ox + col;
+      const float v = w_out[r * pitch + col];
+      if (v != 0.0f && gy < g.n_y && gx < g.n_z) atomicAdd(&out[gy * g.n_z + gx], v);
+    }
+  }
+}
+
+template <int RS, int SW>
+cudaError_t launch_fast_shape(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                              const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
+                              const short4* ev_box, const uint16_t* rows, const float* rho,
+                              float* out, DevCounters* counters, cudaStream_t s) {
+  const size_t smem = 2ull * t.win_w * t.win_h * sizeof(float);
+  cudaError_t err = cudaFuncSetAttribute(iterate_fast_kernel<RS, SW>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+  if (err != cudaSuccess) return err;
+  iterate_fast_kernel<RS, SW><<<n_chunks, t.threads, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box,
+                                                                rows, rho, out, counters);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_row_tables(const DevGeom& g, const Tiling& t, int32_t n_events,
+                              const float4* ev_geom, const short4* ev_box, uint16_t* rows,
+                              unsigned long long* kernel_calls, cudaStream_t s) {
+  if (n_events <= 0) return cudaSuccess;
+  int blocks = (n_events + 7) / 8;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  row_table_kernel<<<blocks, 256, 0, s>>>(g, n_events, t.row_stride, ev_geom, ev_box, rows,
+                                          kernel_calls);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                                const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
+                                const short4* ev_box, const uint16_t* rows, const float* rho,
+                                float* out, DevCounters* counters, cudaStream_t s) {
+  if (n_chunks <= 0) return cudaSuccess;
+  switch (t.fast_shape) {
+    case kShapeS:
+      return launch_fast_shape<4, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out,
+                                     counters, s);
+    case kShapeM:
+      return launch_fast_shape<8, 3>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out,
+                                     counters, s);
+    default:
+      return launch_fast_shape<12, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho,
+                                      out, counters, s);
+  }
+}
+
+}  // namespace jpet

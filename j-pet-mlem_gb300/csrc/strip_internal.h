@@ -35,6 +35,26 @@ struct Tiling {
   int32_t chunk_events;    // events per chunk
   int32_t threads;         // threads per CTA
   int32_t group;           // lanes per image row in the warp rasteriser (8/16/32)
+  int32_t row_stride;      // entries per event in the row table (>= max_box_h, even)
+  int32_t fast_shape;      // register-cache shape of the fast kernel (FastShape)
+};
+
+// Register-cache shapes of the fast iteration kernel: 4 lanes per image row,
+// 8 rows per step, each lane two adjacent pixels per sweep (8 columns per sweep).
+enum FastShape : int32_t {
+  kShapeS = 0,  // <= 32 rows, <= 16 columns per row
+  kShapeM = 1,  // <= 64 rows, <= 24 columns per row
+  kShapeL = 2,  // <= 96 rows, <= 32 columns per row
+};
+
+// Constants of the fast evaluation: the Gaussian kernel written as
+//   K / K_ref = 2^(kz u^2 + ky(sec) dy^2 - 0.5 log2(aMa(py) / aMa(y)))
+// with u = dz - dy tan, dy = py - y (gaussian_kernel.h:51-79 rewritten; the
+// event constant K_ref cancels in K rho / sum K rho).
+struct FastConst {
+  float kz;        // -log2(e) * ipz
+  float kdl;       // -2 log2(e) * ipd   (times sec^2 per event)
+  float two_r2;    // 2 R^2
 };
 
 // Device counters, summed over one iteration.
@@ -61,6 +81,16 @@ cudaError_t launch_scatter_events(int64_t n, const float4* ev_geom, const short4
                                   int32_t* over_cursor, float4* over_geom, short4* over_box,
                                   cudaStream_t s);
 cudaError_t launch_fill(float* p, float v, int64_t n, cudaStream_t s);
+// Exact in-ellipse column interval of every box row of every sorted event
+// (GaussianKernel::in_ellipse evaluated in the reference's rounding),
+// packed as (first column - box.x) | (width << 8); also sums the widths.
+cudaError_t launch_row_tables(const DevGeom& g, const Tiling& t, int32_t n_events,
+                              const float4* ev_geom, const short4* ev_box, uint16_t* rows,
+                              unsigned long long* kernel_calls, cudaStream_t s);
+cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                                const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
+                                const short4* ev_box, const uint16_t* rows, const float* rho,
+                                float* out, DevCounters* counters, cudaStream_t s);
 cudaError_t launch_iterate(const DevGeom& g, const Tiling& t, int32_t semantics,
                            const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                            const short4* ev_box, const float* rho, const float* sens,

@@ -31,6 +31,8 @@ MODE_GPU_REFERENCE = 1
 PRECISION_FP32 = 0
 PRECISION_KAHAN = 1
 PRECISION_FP64_DEN = 2
+VARIANT_FAST = 0
+VARIANT_EXACT = 1
 
 # every symbol include/jpet_strip.h declares
 EXPORTED = [
@@ -70,7 +72,8 @@ class Opts(C.Structure):
         ("tile_w", C.c_int32),
         ("tile_h", C.c_int32),
         ("block_threads", C.c_int32),
-        ("reserved", C.c_int32 * 10),
+        ("variant", C.c_int32),
+        ("reserved", C.c_int32 * 9),
     ]
 
 
@@ -148,11 +151,12 @@ class Geometry:
 
 
 def make_opts(device=0, mode=MODE_CPU_REFERENCE, precision=PRECISION_FP32, tile_w=0,
-              tile_h=0, block_threads=0) -> Opts:
+              tile_h=0, block_threads=0, variant=VARIANT_FAST) -> Opts:
     o = Opts()
     lib().jpet_strip_default_opts(C.byref(o))
     o.device, o.mode, o.precision = device, mode, precision
     o.tile_w, o.tile_h, o.block_threads = tile_w, tile_h, block_threads
+    o.variant = variant
     return o
 
 

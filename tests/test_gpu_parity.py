@@ -13,6 +13,7 @@ from jpet_strip import capi, phantom
 pytestmark = pytest.mark.gpu
 
 TOL_ITER = 1e-5
+VARIANTS = [capi.VARIANT_FAST, capi.VARIANT_EXACT]
 
 
 def rel_l2(a, b):
@@ -25,13 +26,14 @@ def _geoms(c):
     return capi.Geometry(*args), O.Geometry(*args)
 
 
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("case", ["c1", "crop"])
-def test_iterations_match_reference_goldens(golden, case):
+def test_iterations_match_reference_goldens(golden, case, variant):
     manifest, load = golden
     c = manifest[case]
     cg, _ = _geoms(c)
     ev = load(f"{case}_events.npy")
-    with capi.StripReconstruction(cg) as rec:
+    with capi.StripReconstruction(cg, variant=variant) as rec:
         rec.set_events(ev)
         done = 0
         for it in c["iterations"]:
@@ -44,13 +46,14 @@ def test_iterations_match_reference_goldens(golden, case):
         assert rel_l2(got, want) < TOL_ITER
 
 
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("case", ["c1", "crop"])
-def test_each_iteration_and_counters_match_oracle(golden, case):
+def test_each_iteration_and_counters_match_oracle(golden, case, variant):
     manifest, load = golden
     c = manifest[case]
     cg, og = _geoms(c)
     ev = load(f"{case}_events.npy")
-    with capi.StripReconstruction(cg) as rec:
+    with capi.StripReconstruction(cg, variant=variant) as rec:
         rec.set_events(ev)
         rho = None
         for it in range(3):
@@ -65,11 +68,12 @@ def test_each_iteration_and_counters_match_oracle(golden, case):
             rec.rho = rho  # continue both from the same image
 
 
-def test_twenty_iterations_stay_within_1e4(golden):
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_twenty_iterations_stay_within_1e4(golden, variant):
     manifest, load = golden
     cg, og = _geoms(manifest["c1"])
     ev = load("c1_events.npy")
-    with capi.StripReconstruction(cg) as rec:
+    with capi.StripReconstruction(cg, variant=variant) as rec:
         rec.set_events(ev)
         rec.iterate(20)
         got = rec.rho
@@ -110,7 +114,8 @@ def test_empty_event_list_and_iterate_before_events():
         assert not rec.rho.any()
 
 
-def test_edge_events_outside_grid_nan_and_single(golden):
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_edge_events_outside_grid_nan_and_single(golden, variant):
     # events far outside, on the grid corner, NaN and Inf: same result as the oracle
     og = O.Geometry(450, 1000, 90, 100, 5, 10, 42)
     cg = capi.Geometry(450, 1000, 90, 100, 5, 10, 42)
@@ -125,7 +130,7 @@ def test_edge_events_outside_grid_nan_and_single(golden):
         [-249.0, -251.0, -170.0],
     ], np.float32)
     for sl in (slice(0, 1), slice(None)):
-        with capi.StripReconstruction(cg) as rec:
+        with capi.StripReconstruction(cg, variant=variant) as rec:
             rec.set_events(ev[sl])
             rec.iterate(1)
             got = rec.rho
@@ -189,28 +194,29 @@ def test_run_callback_protocol(golden):
     np.testing.assert_allclose(outputs[0][1], O.sensitivity_map(og, 1), rtol=2e-6)
 
 
-def test_forced_small_windows_exercise_large_box_path(golden):
-    # a 1x1 tile with the default window budget still covers every event; a
-    # tiny tile request keeps results identical regardless of the tiling
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_tiling_does_not_change_results(golden, variant):
+    # results are independent of the tile shape (1x1 tiles: one window per pixel)
     manifest, load = golden
     cg, og = _geoms(manifest["c1"])
     ev = load("c1_events.npy")
     want, st = O.mlem_f(og, ev, 1, threads=4)
     for tw, th in [(1, 1), (8, 32), (64, 16)]:
-        with capi.StripReconstruction(cg, tile_w=tw, tile_h=th) as rec:
+        with capi.StripReconstruction(cg, tile_w=tw, tile_h=th, variant=variant) as rec:
             rec.set_events(ev)
             rec.iterate(1)
             assert rel_l2(rec.rho, want) < TOL_ITER
             assert rec.counters()["n_kernel_calls"] == st["n_kernel_calls"]
 
 
-def test_larger_random_phantom_against_oracle():
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_larger_random_phantom_against_oracle(variant):
     # 2 mm grid, 10-ellipse phantom, 30k events
     ell = phantom.random_ellipse_phantom(seed=7)
     ev = phantom.generate_events(ell, 30000, 450.0, 1000.0, 10.0, 42.0, seed=7)
     args = (450.0, 1000.0, 450, 500, 2.0, 10.0, 42.0)
     cg, og = capi.Geometry(*args), O.Geometry(*args)
-    with capi.StripReconstruction(cg) as rec:
+    with capi.StripReconstruction(cg, variant=variant) as rec:
         rec.set_events(ev)
         rho = None
         for _ in range(2):
@@ -219,3 +225,24 @@ def test_larger_random_phantom_against_oracle():
             assert rel_l2(rec.rho, rho) < TOL_ITER
             rec.rho = rho
         assert rec.counters()["n_kernel_calls"] == st["n_kernel_calls"]
+
+
+@pytest.mark.parametrize("sigma", [(5.0, 20.0, 1.0), (14.0, 55.0, 2.0), (10.0, 42.0, 5.0),
+                                   (6.0, 60.0, 3.0)])
+def test_fast_kernel_register_shapes(sigma):
+    # geometries that select each register-cache shape of the fast kernel
+    sz, sdl, p = sigma
+    n_z, n_y = int(1000 / p), int(900 / p)
+    n_z, n_y = min(n_z, 400), min(n_y, 360)
+    ell = phantom.random_ellipse_phantom(seed=3)
+    ev = phantom.generate_events(ell, 8000, 450.0, 1000.0, sz, sdl, seed=3)
+    args = (450.0, 1000.0, n_y, n_z, p, sz, sdl)
+    cg, og = capi.Geometry(*args), O.Geometry(*args)
+    with capi.StripReconstruction(cg) as rec:
+        rec.set_events(ev)
+        rec.iterate(2)
+        got = rec.rho
+        cnt = rec.counters()
+    want, st = O.mlem_f(og, ev, 2, threads=8)
+    assert rel_l2(got, want) < TOL_ITER
+    assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
