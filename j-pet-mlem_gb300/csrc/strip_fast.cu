@@ -133,32 +133,49 @@ constexpr int kG = 4;          // lanes per image row
 constexpr int kRPS = 32 / kG;  // rows per step
 constexpr int kCols = 2 * kG;  // columns per sweep
 
+// Shared-memory window of the fast kernel: origin rounded down to an even
+// column and an even pitch, so that every pixel pair (2k, 2k+1) of a row is one
+// 8-byte aligned ld.shared.v2; 32 floats of padding after the rho window keep
+// the loads of the last sweep of the last row inside the allocation.  The
+// pitch is 8 mod 16 words: the four rows served by one half-warp (4 lanes x 8
+// bytes each) then start in four different groups of 8 banks.
+__host__ __device__ inline int fast_pitch(const Tiling& t) {
+  int p = (t.win_w + 2 + 7) & ~7;
+  return (p % 16 == 8) ? p : p + 8;
+}
+__host__ __device__ inline int fast_window_floats(const Tiling& t) {
+  return t.win_h * fast_pitch(t) + 32;
+}
+
 template <int RS, int SW>
 __global__ void __launch_bounds__(256) iterate_fast_kernel(
     DevGeom g, FastConst fc, Tiling t, const Chunk* __restrict__ chunks,
     const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
     const uint16_t* __restrict__ rows, const float* __restrict__ rho, float* __restrict__ out,
     DevCounters* counters) {
-  extern __shared__ float smem[];
-  const int pitch = t.win_w;
-  const int win = t.win_w * t.win_h;
+  extern __shared__ __align__(16) float smem[];
+  const int pitch = fast_pitch(t);
+  const int wfl = fast_window_floats(t);
   float* w_rho = smem;
-  float* w_out = smem + win;
+  float* w_out = smem + wfl;
   const Chunk c = chunks[blockIdx.x];
+  const int ox = c.ox & ~1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
   for (int r = warp; r < t.win_h; r += n_warps) {
     const int gy = c.oy + r;
-    for (int col = lane; col < t.win_w; col += 32) {
-      const int gx = c.ox + col;
+    for (int col = lane; col < pitch; col += 32) {
+      const int gx = ox + col;
       w_rho[r * pitch + col] = (gy < g.n_y && gx < g.n_z) ? rho[gy * g.n_z + gx] : 0.0f;
       w_out[r * pitch + col] = 0.0f;
     }
   }
+  if (threadIdx.x < 32) w_rho[t.win_h * pitch + threadIdx.x] = 0.0f;
   __syncthreads();
 
   const int gid = lane / kG;  // row of the step this lane works on
   const int gl = lane % kG;   // lane within the row group
-  // per-lane sweep constants: pixel offsets j, j+1 and kz pw^2 j^2
+  // per-lane sweep constants: pixel offsets j, j+1 from the row's first pair
+  // and kz pw^2 j^2
   float2 jf[SW], cj[SW];
   const float kzp2 = fc.kz * g.pixel_width * g.pixel_width;
 #pragma unroll
@@ -168,13 +185,21 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
     cj[s] = make_float2(kzp2 * j0 * j0, kzp2 * (j0 + 1.0f) * (j0 + 1.0f));
   }
   constexpr int kEntRegs = (RS * kRPS + 31) / 32;
+  const float kz2pw = 2.0f * fc.kz * g.pixel_width;
 
-  WindowAccess acc{w_rho, w_out, c.ox, c.oy, pitch};
+  WindowAccess acc{w_rho, w_out, ox, c.oy, pitch};
   unsigned long long contrib = 0, dummy_calls = 0;
-  for (int e = warp; e < c.count; e += n_warps) {
+  int e = warp;
+  float4 ev_next = make_float4(0.f, 0.f, 0.f, 0.f);
+  short4 box_next = make_short4(0, 0, 0, 0);
+  if (e < c.count) {
+    ev_next = ev_geom[c.start + e];
+    box_next = ev_box[c.start + e];
+  }
+  for (; e < c.count; e += n_warps) {
     const int ei = c.start + e;
-    const float4 ev = ev_geom[ei];
-    const short4 box = ev_box[ei];
+    const float4 ev = ev_next;
+    const short4 box = box_next;
     const int nrows = box.w - box.y;
     const uint16_t* rt = rows + static_cast<size_t>(ei) * t.row_stride;
     // the event's row table in registers: lane l holds rows l, l+32, l+64
@@ -186,8 +211,12 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
       ent[k] = (ri < nrows) ? rt[ri] : 0u;
       maxw = max(maxw, static_cast<int>(ent[k] >> 8));
     }
+    if (e + n_warps < c.count) {  // prefetch the next event of this warp
+      ev_next = ev_geom[ei + n_warps];
+      box_next = ev_box[ei + n_warps];
+    }
     maxw = __reduce_max_sync(kFull, maxw);
-    if (nrows > RS * kRPS || maxw > SW * kCols) {
+    if (nrows > RS * kRPS || maxw + 1 > SW * kCols) {
       process_event<kCpuReference>(g, 32, ev, box, acc, nullptr, dummy_calls, contrib);
       continue;
     }
@@ -200,8 +229,12 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
     const float lref = 0.5f * lg2_approx(fmaf(Q, y * y, P));
     const float u_base = g.tl_z_half_w - z;
     const int n_steps = (nrows + kRPS - 1) / kRPS;
+    const int col0 = box.x - ox;  // window column of the box's first column
 
     float2 cache[RS][SW];
+    uint32_t nsw_pack[(RS + 7) / 8];
+#pragma unroll
+    for (int k = 0; k < (RS + 7) / 8; ++k) nsw_pack[k] = 0;
     float2 den2 = make_float2(0.0f, 0.0f);
 #pragma unroll
     for (int rs = 0; rs < RS; ++rs) {
@@ -209,29 +242,36 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
         const int ri = rs * kRPS + gid;
         const uint32_t en = __shfl_sync(kFull, ent[(rs * kRPS) / 32], (rs * kRPS) % 32 + gid);
         const int w = (ri < nrows) ? static_cast<int>(en >> 8) : 0;
-        const int c_lo = box.x + static_cast<int>(en & 255u);
+        const int lo = col0 + static_cast<int>(en & 255u);  // window column of the first pixel
+        const int a_off = lo & ~1;                          // its aligned pair
+        const int d = lo + w - a_off - 2 * gl;              // elements left for this lane
+        const bool lo_skip = (gl == 0) && (lo & 1);
+        const int row = min(ri, nrows - 1) + box.y - c.oy;
+        int nsw = w > 0 ? (lo + w - a_off + kCols - 1) / kCols : 0;
+        nsw = __reduce_max_sync(kFull, nsw);
+        nsw_pack[rs / 8] |= static_cast<uint32_t>(nsw) << (4 * (rs % 8));
         const int iy = box.y + ri;
         const float py = g.tl_y_half_h - static_cast<float>(iy) * g.pixel_height;
         const float dy = py - y;
         const float lf = lref - 0.5f * lg2_approx(fmaf(Q, py * py, P));
-        const float u0 = fmaf(static_cast<float>(c_lo), g.pixel_width, u_base - dy * tn);
-        const float p_row = fmaf(fc.kz * u0, u0, fmaf(ky * dy, dy, lf));
-        const float q_row = 2.0f * fc.kz * g.pixel_width * u0;
-        const float* rp = w_rho + (iy - c.oy) * pitch + (c_lo - c.ox);
+        const float ua = fmaf(static_cast<float>(ox + a_off), g.pixel_width, u_base - dy * tn);
+        const float p_row = fmaf(fc.kz * ua, ua, fmaf(ky * dy, dy, lf));
+        const float q_row = kz2pw * ua;
+        const float2 p2 = make_float2(p_row, p_row), q2 = make_float2(q_row, q_row);
+        const float* rp = w_rho + row * pitch + a_off + 2 * gl;
 #pragma unroll
         for (int s = 0; s < SW; ++s) {
-          const int j = 2 * gl + kCols * s;
-          float2 kr = make_float2(0.0f, 0.0f);
-          if (j < w) {
-            const float2 a = __ffma2_rn(make_float2(q_row, q_row), jf[s],
-                                        __fadd2_rn(make_float2(p_row, p_row), cj[s]));
-            const float2 ex = make_float2(ex2_approx(a.x), ex2_approx(a.y));
-            const float2 r2 = make_float2(rp[j], rp[j + 1]);
-            kr = __fmul2_rn(ex, r2);
-            if (j + 1 >= w) kr.y = 0.0f;
+          if (s < nsw) {
+            const float2 a = __ffma2_rn(q2, jf[s], __fadd2_rn(p2, cj[s]));
+            const float2 r2 = *reinterpret_cast<const float2*>(rp + kCols * s);
+            float2 kr = __fmul2_rn(make_float2(ex2_approx(a.x), ex2_approx(a.y)), r2);
+            const bool v0 = (kCols * s < d) && !(s == 0 && lo_skip);
+            const bool v1 = (kCols * s + 1 < d);
+            kr.x = v0 ? kr.x : 0.0f;
+            kr.y = v1 ? kr.y : 0.0f;
+            cache[rs][s] = kr;
+            den2 = __fadd2_rn(den2, kr);
           }
-          cache[rs][s] = kr;
-          den2 = __fadd2_rn(den2, kr);
         }
       }
     }
@@ -245,16 +285,17 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
       if (rs < n_steps) {
         const int ri = rs * kRPS + gid;
         const uint32_t en = __shfl_sync(kFull, ent[(rs * kRPS) / 32], (rs * kRPS) % 32 + gid);
-        const int w = (ri < nrows) ? static_cast<int>(en >> 8) : 0;
-        const int c_lo = box.x + static_cast<int>(en & 255u);
-        float* op = w_out + (box.y + ri - c.oy) * pitch + (c_lo - c.ox);
+        const int lo = col0 + static_cast<int>(en & 255u);
+        const int a_off = lo & ~1;
+        const int row = min(ri, nrows - 1) + box.y - c.oy;
+        const int nsw = static_cast<int>((nsw_pack[rs / 8] >> (4 * (rs % 8))) & 15u);
+        float* op = w_out + row * pitch + a_off + 2 * gl;
 #pragma unroll
         for (int s = 0; s < SW; ++s) {
-          const int j = 2 * gl + kCols * s;
-          if (j < w) {
+          if (s < nsw) {
             const float2 v = __fmul2_rn(cache[rs][s], inv2);
-            atomicAdd(op + j, v.x);
-            if (j + 1 < w) atomicAdd(op + j + 1, v.y);
+            if (v.x != 0.0f) atomicAdd(op + kCols * s, v.x);
+            if (v.y != 0.0f) atomicAdd(op + kCols * s + 1, v.y);
           }
         }
       }
@@ -264,8 +305,8 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
   __syncthreads();
   for (int r = warp; r < t.win_h; r += n_warps) {
     const int gy = c.oy + r;
-    for (int col = lane; col < t.win_w; col += 32) {
-      const int gx = c.ox + col;
+    for (int col = lane; col < pitch; col += 32) {
+      const int gx = ox + col;
       const float v = w_out[r * pitch + col];
       if (v != 0.0f && gy < g.n_y && gx < g.n_z) atomicAdd(&out[gy * g.n_z + gx], v);
     }
@@ -277,7 +318,7 @@ cudaError_t launch_fast_shape(const DevGeom& g, const FastConst& fc, const Tilin
                               const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                               const short4* ev_box, const uint16_t* rows, const float* rho,
                               float* out, DevCounters* counters, cudaStream_t s) {
-  const size_t smem = 2ull * t.win_w * t.win_h * sizeof(float);
+  const size_t smem = 2ull * fast_window_floats(t) * sizeof(float);
   cudaError_t err = cudaFuncSetAttribute(iterate_fast_kernel<RS, SW>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
