@@ -135,16 +135,118 @@ constexpr int kCols = 2 * kG;  // columns per sweep
 
 // Shared-memory window of the fast kernel: origin rounded down to an even
 // column and an even pitch, so that every pixel pair (2k, 2k+1) of a row is one
-// 8-byte aligned ld.shared.v2; 32 floats of padding after the rho window keep
-// the loads of the last sweep of the last row inside the allocation.  The
-// pitch is 8 mod 16 words: the four rows served by one half-warp (4 lanes x 8
-// bytes each) then start in four different groups of 8 banks.
+// 8-byte aligned ld.shared.v2; 64 floats of padding after the rho window keep
+// the unconditional loads of the last row inside the allocation.  The pitch is
+// 8 mod 16 words: the four rows served by one half-warp (4 lanes x 8 bytes
+// each) then start in four different groups of 8 banks.
 __host__ __device__ inline int fast_pitch(const Tiling& t) {
   int p = (t.win_w + 2 + 7) & ~7;
   return (p % 16 == 8) ? p : p + 8;
 }
 __host__ __device__ inline int fast_window_floats(const Tiling& t) {
-  return t.win_h * fast_pitch(t) + 32;
+  return t.win_h * fast_pitch(t) + 64;
+}
+
+struct FastLane {
+  float2 jf[4], cj[4];  // per-lane pixel offsets j, j+1 and kz pw^2 j^2 per sweep
+};
+
+// One event on one warp, straight-line code for RS row steps x SW sweeps:
+// phase A computes the constants of 32 rows per pass (one row per lane), phase
+// B evaluates every (row step, sweep) slot without branches (invalid pixels
+// are zeroed), phase C adds K rho / den with shared-memory atomics.
+// Returns whether the event contributed (den > 0).
+template <int RS, int SW>
+__device__ __forceinline__ bool fast_event(const DevGeom& g, const FastConst& fc, float4 ev,
+                                           short4 box, const uint32_t* ent, int nrows, int ox,
+                                           int oy, int pitch, const float* w_rho, float* w_out,
+                                           const FastLane& fl) {
+  constexpr int kSets = (RS * kRPS + 31) / 32;
+  const int lane = threadIdx.x & 31;
+  const int gid = lane / kG, gl = lane % kG;
+  const float z = ev.x, y = ev.y, tn = ev.z, sec = ev.w;
+  const float sec2 = sec * sec;
+  const float ky = fc.kdl * sec2;
+  // aMa(py) = P + Q py^2
+  const float P = fc.two_r2 * sec2 * sec2 * g.ipz;
+  const float Q = 2.0f * sec2 * sec2 * g.ipz + 4.0f * sec2 * tn * tn * g.ipd;
+  const float lref = 0.5f * lg2_approx(fmaf(Q, y * y, P));
+  const float u_base = g.tl_z_half_w - z;
+  const int col0 = box.x - ox;
+  const float kz2pw = 2.0f * fc.kz * g.pixel_width;
+
+  // phase A: row constants, lane l <- rows l, l + 32, ...
+  int rw[kSets], rb[kSets];
+  float rpv[kSets], rqv[kSets];
+#pragma unroll
+  for (int k = 0; k < kSets; ++k) {
+    const int ri = lane + 32 * k;
+    const uint32_t en = ent[k];
+    const int w = (ri < nrows) ? static_cast<int>(en >> 8) : 0;
+    const int lo = col0 + static_cast<int>(en & 255u);
+    const int a_off = lo & ~1;
+    const int row = min(ri, nrows - 1) + box.y - oy;
+    const float py = g.tl_y_half_h - static_cast<float>(box.y + ri) * g.pixel_height;
+    const float dy = py - y;
+    const float lf = lref - 0.5f * lg2_approx(fmaf(Q, py * py, P));
+    const float ua = fmaf(static_cast<float>(ox + a_off), g.pixel_width, u_base - dy * tn);
+    rw[k] = w | ((lo & 1) << 8);
+    rb[k] = row * pitch + a_off;
+    rpv[k] = fmaf(fc.kz * ua, ua, fmaf(ky * dy, dy, lf));
+    rqv[k] = kz2pw * ua;
+  }
+
+  // phase B: forward sum over all slots
+  float2 cache[RS][SW];
+  float2 den_a = make_float2(0.0f, 0.0f), den_b = make_float2(0.0f, 0.0f);
+#pragma unroll
+  for (int rs = 0; rs < RS; ++rs) {
+    const int src = (rs * kRPS) % 32 + gid;
+    const int set = (rs * kRPS) / 32;
+    const int wl = __shfl_sync(kFull, rw[set], src);
+    const int base = __shfl_sync(kFull, rb[set], src);
+    const float p = __shfl_sync(kFull, rpv[set], src);
+    const float q = __shfl_sync(kFull, rqv[set], src);
+    const int lodd = (wl >> 8) & 1;
+    const int d = (wl & 255) + lodd - 2 * gl;  // elements of the row left for this lane
+    const bool lo_skip = (gl == 0) && lodd;
+    const float* rp = w_rho + base + 2 * gl;
+    const float2 p2 = make_float2(p, p), q2 = make_float2(q, q);
+#pragma unroll
+    for (int s = 0; s < SW; ++s) {
+      const float2 a = __ffma2_rn(q2, fl.jf[s], __fadd2_rn(p2, fl.cj[s]));
+      const float2 r2 = *reinterpret_cast<const float2*>(rp + kCols * s);
+      float2 kr = __fmul2_rn(make_float2(ex2_approx(a.x), ex2_approx(a.y)), r2);
+      const bool v0 = (kCols * s < d) && !(s == 0 && lo_skip);
+      const bool v1 = (kCols * s + 1 < d);
+      kr.x = v0 ? kr.x : 0.0f;
+      kr.y = v1 ? kr.y : 0.0f;
+      cache[rs][s] = kr;
+      if (rs & 1)
+        den_b = __fadd2_rn(den_b, kr);
+      else
+        den_a = __fadd2_rn(den_a, kr);
+    }
+  }
+  const float den = warp_sum((den_a.x + den_a.y) + (den_b.x + den_b.y));
+  if (!(den > 0.0f)) return false;  // inv_denominator = 0 (reconstruction.h:290)
+  const float inv = __fdiv_rn(1.0f, den);
+  const float2 inv2 = make_float2(inv, inv);
+  // phase C: back-projection
+#pragma unroll
+  for (int rs = 0; rs < RS; ++rs) {
+    const int src = (rs * kRPS) % 32 + gid;
+    const int set = (rs * kRPS) / 32;
+    const int base = __shfl_sync(kFull, rb[set], src);
+    float* op = w_out + base + 2 * gl;
+#pragma unroll
+    for (int s = 0; s < SW; ++s) {
+      const float2 v = __fmul2_rn(cache[rs][s], inv2);
+      if (v.x != 0.0f) atomicAdd(op + kCols * s, v.x);
+      if (v.y != 0.0f) atomicAdd(op + kCols * s + 1, v.y);
+    }
+  }
+  return true;
 }
 
 template <int RS, int SW>
@@ -169,24 +271,21 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
       w_out[r * pitch + col] = 0.0f;
     }
   }
-  if (threadIdx.x < 32) w_rho[t.win_h * pitch + threadIdx.x] = 0.0f;
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) w_rho[t.win_h * pitch + i] = 0.0f;
   __syncthreads();
 
-  const int gid = lane / kG;  // row of the step this lane works on
-  const int gl = lane % kG;   // lane within the row group
-  // per-lane sweep constants: pixel offsets j, j+1 from the row's first pair
-  // and kz pw^2 j^2
-  float2 jf[SW], cj[SW];
-  const float kzp2 = fc.kz * g.pixel_width * g.pixel_width;
+  FastLane fl;
+  {
+    const int gl = lane % kG;
+    const float kzp2 = fc.kz * g.pixel_width * g.pixel_width;
 #pragma unroll
-  for (int s = 0; s < SW; ++s) {
-    const float j0 = static_cast<float>(2 * gl + kCols * s);
-    jf[s] = make_float2(j0, j0 + 1.0f);
-    cj[s] = make_float2(kzp2 * j0 * j0, kzp2 * (j0 + 1.0f) * (j0 + 1.0f));
+    for (int s = 0; s < SW; ++s) {
+      const float j0 = static_cast<float>(2 * gl + kCols * s);
+      fl.jf[s] = make_float2(j0, j0 + 1.0f);
+      fl.cj[s] = make_float2(kzp2 * j0 * j0, kzp2 * (j0 + 1.0f) * (j0 + 1.0f));
+    }
   }
   constexpr int kEntRegs = (RS * kRPS + 31) / 32;
-  const float kz2pw = 2.0f * fc.kz * g.pixel_width;
-
   WindowAccess acc{w_rho, w_out, ox, c.oy, pitch};
   unsigned long long contrib = 0, dummy_calls = 0;
   int e = warp;
@@ -202,7 +301,6 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
     const short4 box = box_next;
     const int nrows = box.w - box.y;
     const uint16_t* rt = rows + static_cast<size_t>(ei) * t.row_stride;
-    // the event's row table in registers: lane l holds rows l, l+32, l+64
     uint32_t ent[kEntRegs];
     int maxw = 0;
 #pragma unroll
@@ -216,90 +314,17 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
       box_next = ev_box[ei + n_warps];
     }
     maxw = __reduce_max_sync(kFull, maxw);
+    bool ok;
     if (nrows > RS * kRPS || maxw + 1 > SW * kCols) {
       process_event<kCpuReference>(g, 32, ev, box, acc, nullptr, dummy_calls, contrib);
       continue;
+    } else if (RS > 4 && nrows <= (RS / 2) * kRPS) {
+      ok = fast_event<(RS > 4 ? RS / 2 : RS), SW>(g, fc, ev, box, ent, nrows, ox, c.oy, pitch,
+                                                  w_rho, w_out, fl);
+    } else {
+      ok = fast_event<RS, SW>(g, fc, ev, box, ent, nrows, ox, c.oy, pitch, w_rho, w_out, fl);
     }
-    const float z = ev.x, y = ev.y, tn = ev.z, sec = ev.w;
-    const float sec2 = sec * sec;
-    const float ky = fc.kdl * sec2;
-    // aMa(py) = P + Q py^2
-    const float P = fc.two_r2 * sec2 * sec2 * g.ipz;
-    const float Q = 2.0f * sec2 * sec2 * g.ipz + 4.0f * sec2 * tn * tn * g.ipd;
-    const float lref = 0.5f * lg2_approx(fmaf(Q, y * y, P));
-    const float u_base = g.tl_z_half_w - z;
-    const int n_steps = (nrows + kRPS - 1) / kRPS;
-    const int col0 = box.x - ox;  // window column of the box's first column
-
-    float2 cache[RS][SW];
-    uint32_t nsw_pack[(RS + 7) / 8];
-#pragma unroll
-    for (int k = 0; k < (RS + 7) / 8; ++k) nsw_pack[k] = 0;
-    float2 den2 = make_float2(0.0f, 0.0f);
-#pragma unroll
-    for (int rs = 0; rs < RS; ++rs) {
-      if (rs < n_steps) {
-        const int ri = rs * kRPS + gid;
-        const uint32_t en = __shfl_sync(kFull, ent[(rs * kRPS) / 32], (rs * kRPS) % 32 + gid);
-        const int w = (ri < nrows) ? static_cast<int>(en >> 8) : 0;
-        const int lo = col0 + static_cast<int>(en & 255u);  // window column of the first pixel
-        const int a_off = lo & ~1;                          // its aligned pair
-        const int d = lo + w - a_off - 2 * gl;              // elements left for this lane
-        const bool lo_skip = (gl == 0) && (lo & 1);
-        const int row = min(ri, nrows - 1) + box.y - c.oy;
-        int nsw = w > 0 ? (lo + w - a_off + kCols - 1) / kCols : 0;
-        nsw = __reduce_max_sync(kFull, nsw);
-        nsw_pack[rs / 8] |= static_cast<uint32_t>(nsw) << (4 * (rs % 8));
-        const int iy = box.y + ri;
-        const float py = g.tl_y_half_h - static_cast<float>(iy) * g.pixel_height;
-        const float dy = py - y;
-        const float lf = lref - 0.5f * lg2_approx(fmaf(Q, py * py, P));
-        const float ua = fmaf(static_cast<float>(ox + a_off), g.pixel_width, u_base - dy * tn);
-        const float p_row = fmaf(fc.kz * ua, ua, fmaf(ky * dy, dy, lf));
-        const float q_row = kz2pw * ua;
-        const float2 p2 = make_float2(p_row, p_row), q2 = make_float2(q_row, q_row);
-        const float* rp = w_rho + row * pitch + a_off + 2 * gl;
-#pragma unroll
-        for (int s = 0; s < SW; ++s) {
-          if (s < nsw) {
-            const float2 a = __ffma2_rn(q2, jf[s], __fadd2_rn(p2, cj[s]));
-            const float2 r2 = *reinterpret_cast<const float2*>(rp + kCols * s);
-            float2 kr = __fmul2_rn(make_float2(ex2_approx(a.x), ex2_approx(a.y)), r2);
-            const bool v0 = (kCols * s < d) && !(s == 0 && lo_skip);
-            const bool v1 = (kCols * s + 1 < d);
-            kr.x = v0 ? kr.x : 0.0f;
-            kr.y = v1 ? kr.y : 0.0f;
-            cache[rs][s] = kr;
-            den2 = __fadd2_rn(den2, kr);
-          }
-        }
-      }
-    }
-    const float den = warp_sum(den2.x + den2.y);
-    if (!(den > 0.0f)) continue;  // inv_denominator = 0 (reconstruction.h:290)
-    if (lane == 0) ++contrib;
-    const float inv = __fdiv_rn(1.0f, den);
-    const float2 inv2 = make_float2(inv, inv);
-#pragma unroll
-    for (int rs = 0; rs < RS; ++rs) {
-      if (rs < n_steps) {
-        const int ri = rs * kRPS + gid;
-        const uint32_t en = __shfl_sync(kFull, ent[(rs * kRPS) / 32], (rs * kRPS) % 32 + gid);
-        const int lo = col0 + static_cast<int>(en & 255u);
-        const int a_off = lo & ~1;
-        const int row = min(ri, nrows - 1) + box.y - c.oy;
-        const int nsw = static_cast<int>((nsw_pack[rs / 8] >> (4 * (rs % 8))) & 15u);
-        float* op = w_out + row * pitch + a_off + 2 * gl;
-#pragma unroll
-        for (int s = 0; s < SW; ++s) {
-          if (s < nsw) {
-            const float2 v = __fmul2_rn(cache[rs][s], inv2);
-            if (v.x != 0.0f) atomicAdd(op + kCols * s, v.x);
-            if (v.y != 0.0f) atomicAdd(op + kCols * s + 1, v.y);
-          }
-        }
-      }
-    }
+    if (ok && lane == 0) ++contrib;
   }
   if (lane == 0 && contrib) atomicAdd(&counters->n_contributing, contrib);
   __syncthreads();
