@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-peaks", action="store_true", help="skip the peak microbenchmarks")
     p.add_argument("--variant", type=int, default=0, help="0 fast kernel, 1 exact kernel")
+    p.add_argument("--precision", type=int, default=0,
+                   help="0 FP32 tile sums, 1 compensated (exact) tile sums, 2 plus FP64 denominators")
     return p.parse_args()
 
 
@@ -118,14 +120,15 @@ class ClockSampler:
 
 def measured_peaks(device: int):
     lib = C.CDLL(os.path.join(PKG, "lib", "libjpet_peaks.so"))
-    out = (C.c_double * 9)()
+    out = (C.c_double * 12)()
     rc = lib.jpet_peaks_measure(device, out)
     if rc != 0:
         raise RuntimeError(f"peak microbenchmark failed: {rc}")
     return {"ex2_per_s": out[0], "ffma_per_s": out[1], "shared_atomic_per_s": out[2],
             "global_atomic_per_s": out[3], "sms": int(out[4]), "sm_clock_khz": int(out[5]),
             "shared_atomic_u32_per_s": out[6], "shared_atomic_u64_per_s": out[7],
-            "shared_rmw_per_s": out[8]}
+            "shared_rmw_per_s": out[8], "global_atomic_v4_floats_per_s": out[9],
+            "global_atomic_v2_floats_per_s": out[10], "shared_ld64_floats_per_s": out[11]}
 
 
 def hbm_peak():
@@ -213,7 +216,8 @@ def gb300_arm(args, wl, world, rank, local):
     geom = capi.Geometry(*wl.geometry_args())
     peaks = None if args.no_peaks else measured_peaks(local)
     stream = torch.cuda.Stream()
-    rec = capi.StripReconstruction(geom, device=local, variant=args.variant)
+    rec = capi.StripReconstruction(geom, device=local, variant=args.variant,
+                                   precision=args.precision)
     rec.set_stream(stream.cuda_stream)
     rec.set_events(events)
     with torch.cuda.stream(stream):
@@ -255,7 +259,8 @@ def gb300_arm(args, wl, world, rank, local):
 
         og = oracle.Geometry(*wl.geometry_args())
         sample = events[:200000]
-        with capi.StripReconstruction(geom, device=local) as r2:
+        with capi.StripReconstruction(geom, device=local, variant=args.variant,
+                                      precision=args.precision) as r2:
             r2.set_events(sample)
             r2.iterate(1)
             got = r2.rho.astype(np.float64)
@@ -317,6 +322,8 @@ def gb300_arm(args, wl, world, rank, local):
                     "traffic": None, "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_kind}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "kernel": {"variant": ["fast", "exact"][args.variant],
+                   "precision": ["fp32", "compensated", "fp64_den"][args.precision]},
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl.name, "events": n_events, "grid": f"{wl.n_z}x{wl.n_y}",

@@ -61,10 +61,17 @@ typedef struct jpet_strip_geom {
 #define JPET_MODE_CPU_REFERENCE 0 /* GaussianKernel, no sensitivity: reconstruction.h:220-298 */
 #define JPET_MODE_GPU_REFERENCE 1 /* AnalyticKernel, denominator weighted by the 5-point
                                      pixel sensitivity: warp_granularity.cuh:19-155 */
-/* accumulation precision */
-#define JPET_PRECISION_FP32 0       /* FP32 evaluation, FP32 shared-memory tile sums */
-#define JPET_PRECISION_KAHAN 1      /* FP32 evaluation, compensated per-tile sums */
-#define JPET_PRECISION_FP64_DEN 2   /* as KAHAN, plus per-event denominators reduced in FP64 */
+/* accumulation precision (fast kernel; the exact kernel and the GPU-reference
+ * mode accumulate in FP32) */
+#define JPET_PRECISION_FP32 0        /* FP32 evaluation, FP32 shared-memory tile sums, FP32 image */
+#define JPET_PRECISION_COMPENSATED 1 /* FP32 evaluation; per-tile sums are error-free: each
+                                        contribution is rounded once to 2^-22 of an event
+                                        (unbiased dither) and summed in integers, tiles are
+                                        added into an FP64 image.  This plays the role of a
+                                        Kahan correction, which shared-memory atomics cannot
+                                        carry, and is independent of the summation order */
+#define JPET_PRECISION_FP64_DEN 2    /* as COMPENSATED, plus per-event denominators reduced
+                                        in FP64 */
 
 /* iteration kernel */
 #define JPET_VARIANT_FAST 0  /* exp2-form kernel, packed f32x2, register-cached K*rho (default) */

@@ -128,6 +128,36 @@ __global__ void red_kernel(float* buf, int iters, int mask) {
   }
 }
 
+// global vector atomics (sm_90+): red.global.add.v4.f32 / v2.f32
+__global__ void red_v4_kernel(float4* buf, int iters, int mask4) {
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x);
+  const float4 one = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+  for (int i = 0; i < iters; ++i) atomicAdd(&buf[(t + i * 4096) & mask4], one);
+}
+
+__global__ void red_v2_kernel(float2* buf, int iters, int mask2) {
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x);
+  const float2 one = make_float2(1.0f, 1.0f);
+  for (int i = 0; i < iters; ++i) atomicAdd(&buf[(t + i * 4096) & mask2], one);
+}
+
+// conflict-free ld.shared.v2 throughput (elements per second)
+__global__ void lds64_kernel(float* out, int iters) {
+  __shared__ float2 sm[1024];
+  for (int i = threadIdx.x; i < 1024; i += blockDim.x) sm[i] = make_float2(i, i);
+  __syncthreads();
+  float2 acc = make_float2(0.f, 0.f);
+  int k = threadIdx.x;
+  for (int i = 0; i < iters; ++i) {
+    const float2 a = sm[(k + 0) & 1023], b = sm[(k + 256) & 1023], c = sm[(k + 512) & 1023],
+                 d = sm[(k + 768) & 1023];
+    acc.x += a.x + b.x + c.x + d.x;
+    acc.y += a.y + b.y + c.y + d.y;
+    k += 32;
+  }
+  if (acc.x == -1.0f) out[threadIdx.x] = acc.y;
+}
+
 template <class F>
 double best_rate(F launch, double ops, int reps) {
   cudaEvent_t a, b;
@@ -156,7 +186,9 @@ extern "C" {
 // out[0] ex2/s, out[1] ffma/s, out[2] shared float atomics/s, out[3] global
 // float atomics/s, out[4] number of SMs, out[5] SM clock (kHz, device
 // attribute), out[6] shared u32 atomics/s, out[7] shared u64 atomics/s,
-// out[8] plain shared read-modify-writes/s.  Returns 0 or a CUDA error code.
+// out[8] plain shared read-modify-writes/s, out[9] global float4 atomics
+// (floats/s), out[10] global float2 atomics (floats/s), out[11] conflict-free
+// ld.shared.v2 (floats/s).  Returns 0 or a CUDA error code.
 int jpet_peaks_measure(int device, double* out) {
   if (cudaSetDevice(device) != cudaSuccess) return 1;
   int sms = 0, clk = 0;
@@ -186,6 +218,14 @@ int jpet_peaks_measure(int device, double* out) {
                      double(blocks) * threads * it_ats * 4, 5);
   out[8] = best_rate([&] { rmw_kernel<<<blocks, threads>>>(buf, it_ats); },
                      double(blocks) * threads * it_ats * 4, 5);
+  out[9] = best_rate([&] { red_v4_kernel<<<blocks, threads>>>(reinterpret_cast<float4*>(buf),
+                                                              it_red, (mask + 1) / 4 - 1); },
+                     double(blocks) * threads * it_red * 4, 5);
+  out[10] = best_rate([&] { red_v2_kernel<<<blocks, threads>>>(reinterpret_cast<float2*>(buf),
+                                                               it_red, (mask + 1) / 2 - 1); },
+                      double(blocks) * threads * it_red * 2, 5);
+  out[11] = best_rate([&] { lds64_kernel<<<blocks, threads>>>(buf, it_ats); },
+                      double(blocks) * threads * it_ats * 8, 5);
   cudaError_t e = cudaDeviceSynchronize();
   cudaFree(buf);
   return e == cudaSuccess ? 0 : static_cast<int>(e);

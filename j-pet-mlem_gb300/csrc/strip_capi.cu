@@ -61,6 +61,7 @@ struct jpet_strip {
   std::string last_error = "no error";
 
   DevBuf<float> rho, out, sens_point, sens_pixel;
+  DevBuf<double> out64;              // FP64 image of the compensated modes
   DevBuf<float> raw;                 // staging for uploaded SoA events
   DevBuf<float4> ev_geom, sorted_geom, over_geom;
   DevBuf<short4> ev_box, sorted_box, over_box;
@@ -401,8 +402,14 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
     g_create_error = "unknown kernel variant";
     return JPET_ERR_ARGUMENT;
   }
-  if (o.precision != JPET_PRECISION_FP32) {
-    g_create_error = "precision mode not available in this build";
+  if (o.precision != JPET_PRECISION_FP32 && o.precision != JPET_PRECISION_COMPENSATED &&
+      o.precision != JPET_PRECISION_FP64_DEN) {
+    g_create_error = "unknown precision mode";
+    return JPET_ERR_ARGUMENT;
+  }
+  if (o.precision != JPET_PRECISION_FP32 &&
+      (o.mode != JPET_MODE_CPU_REFERENCE || o.variant != JPET_VARIANT_FAST)) {
+    g_create_error = "compensated precision modes need the fast kernel and the CPU-reference mode";
     return JPET_ERR_UNSUPPORTED;
   }
   int n_dev = 0;
@@ -440,7 +447,8 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
   }
   h->stream = h->own_stream;
   const size_t n_pix = static_cast<size_t>(h->g.n_y) * h->g.n_z;
-  if (h->rho.alloc(n_pix) != cudaSuccess || h->out.alloc(n_pix) != cudaSuccess ||
+  if ((o.precision != JPET_PRECISION_FP32 && h->out64.alloc(n_pix) != cudaSuccess) ||
+      h->rho.alloc(n_pix) != cudaSuccess || h->out.alloc(n_pix) != cudaSuccess ||
       h->sens_point.alloc(n_pix) != cudaSuccess || h->sens_pixel.alloc(n_pix) != cudaSuccess ||
       h->counters.alloc(1) != cudaSuccess) {
     g_create_error = "cudaMalloc(images) failed";
@@ -467,6 +475,7 @@ int jpet_strip_destroy(jpet_strip_t* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   h->rho.release();
   h->out.release();
+  h->out64.release();
   h->sens_point.release();
   h->sens_pixel.release();
   h->raw.release();
@@ -558,10 +567,18 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
   for (int it = 0; it < n; ++it) {
     JPET_CUDA(h, cudaMemsetAsync(h->out.p, 0, n_pix * sizeof(float), s), "clear image");
     JPET_CUDA(h, cudaMemsetAsync(h->counters.p, 0, sizeof(DevCounters), s), "clear counters");
+    const bool fixed = h->opts.precision != JPET_PRECISION_FP32;
+    if (fixed)
+      JPET_CUDA(h, cudaMemsetAsync(h->out64.p, 0, n_pix * sizeof(double), s), "clear image");
     if (h->use_fast) {
+      const int prec = h->opts.precision == JPET_PRECISION_COMPENSATED ? kPrecisionFixed
+                       : h->opts.precision == JPET_PRECISION_FP64_DEN  ? kPrecisionFixedDen64
+                                                                       : kPrecisionFloat;
+      const uint32_t seed = 0x9E3779B9u * static_cast<uint32_t>(h->iterations_done + 1);
       JPET_CUDA(h, launch_iterate_fast(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
                                        h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
-                                       h->rho.p, h->out.p, h->counters.p, s),
+                                       h->rho.p, h->out.p, h->out64.p, h->counters.p, prec, seed,
+                                       s),
                 "iteration kernel launch");
     } else {
       JPET_CUDA(h, launch_iterate(h->g, h->tiling, h->opts.mode, h->chunks.p, h->n_chunks,
@@ -572,6 +589,9 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
     JPET_CUDA(h, launch_iterate_global(h->g, h->opts.mode, h->n_oversize, h->over_geom.p,
                                        h->over_box.p, h->rho.p, sens, h->out.p, h->counters.p, s),
               "large-box kernel launch");
+    if (fixed)
+      JPET_CUDA(h, launch_combine_fixed(h->out64.p, h->out.p, h->out.p, n_pix, s),
+                "combine kernel launch");
     std::swap(h->rho, h->out);
     ++h->iterations_done;
     h->counters_valid = true;

@@ -151,16 +151,38 @@ struct FastLane {
   float2 jf[4], cj[4];  // per-lane pixel offsets j, j+1 and kz pw^2 j^2 per sweep
 };
 
+// Accumulation of the back-projection window.
+//   kAccFloat: float shared-memory atomics (red.shared.add.f32)
+//   kAccFixed: each contribution (a fraction of one event, in [0, 1]) rounded to
+//              22 fractional bits with an unbiased per-event dither and added
+//              with integer shared atomics; a window pixel of a chunk of <= 512
+//              events then stays below 2^31, and its sum is exact and
+//              independent of the order of the additions.
+enum Acc : int { kAccFloat = 0, kAccFixed = 1 };
+constexpr float kFixedScale = 4194304.0f;     // 2^22
+constexpr float kMagic = 12582912.0f;         // 1.5 * 2^23: float -> integer rounding
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+  // integer finaliser of MurmurHash3 (public domain, Austin Appleby)
+  x ^= x >> 16;
+  x *= 0x85ebca6bu;
+  x ^= x >> 13;
+  x *= 0xc2b2ae35u;
+  x ^= x >> 16;
+  return x;
+}
+
 // One event on one warp, straight-line code for RS row steps x SW sweeps:
 // phase A computes the constants of 32 rows per pass (one row per lane), phase
 // B evaluates every (row step, sweep) slot without branches (invalid pixels
 // are zeroed), phase C adds K rho / den with shared-memory atomics.
+// DEN64 reduces the per-lane partial denominators in FP64.
 // Returns whether the event contributed (den > 0).
-template <int RS, int SW>
+template <int RS, int SW, int ACC, bool DEN64>
 __device__ __forceinline__ bool fast_event(const DevGeom& g, const FastConst& fc, float4 ev,
                                            short4 box, const uint32_t* ent, int nrows, int ox,
                                            int oy, int pitch, const float* w_rho, float* w_out,
-                                           const FastLane& fl) {
+                                           const FastLane& fl, uint32_t dither_key) {
   constexpr int kSets = (RS * kRPS + 31) / 32;
   const int lane = threadIdx.x & 31;
   const int gid = lane / kG, gl = lane % kG;
@@ -228,33 +250,67 @@ __device__ __forceinline__ bool fast_event(const DevGeom& g, const FastConst& fc
         den_a = __fadd2_rn(den_a, kr);
     }
   }
-  const float den = warp_sum((den_a.x + den_a.y) + (den_b.x + den_b.y));
+  float den;
+  if (DEN64) {
+    double dd = static_cast<double>(den_a.x + den_a.y) + static_cast<double>(den_b.x + den_b.y);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dd += __shfl_xor_sync(kFull, dd, o);
+    den = static_cast<float>(dd);
+    if (!(dd > 0.0)) return false;
+  } else {
+    den = warp_sum((den_a.x + den_a.y) + (den_b.x + den_b.y));
+  }
   if (!(den > 0.0f)) return false;  // inv_denominator = 0 (reconstruction.h:290)
   const float inv = __fdiv_rn(1.0f, den);
-  const float2 inv2 = make_float2(inv, inv);
   // phase C: back-projection
+  if (ACC == kAccFloat) {
+    const float2 inv2 = make_float2(inv, inv);
 #pragma unroll
-  for (int rs = 0; rs < RS; ++rs) {
-    const int src = (rs * kRPS) % 32 + gid;
-    const int set = (rs * kRPS) / 32;
-    const int base = __shfl_sync(kFull, rb[set], src);
-    float* op = w_out + base + 2 * gl;
+    for (int rs = 0; rs < RS; ++rs) {
+      const int src = (rs * kRPS) % 32 + gid;
+      const int set = (rs * kRPS) / 32;
+      const int base = __shfl_sync(kFull, rb[set], src);
+      float* op = w_out + base + 2 * gl;
 #pragma unroll
-    for (int s = 0; s < SW; ++s) {
-      const float2 v = __fmul2_rn(cache[rs][s], inv2);
-      if (v.x != 0.0f) atomicAdd(op + kCols * s, v.x);
-      if (v.y != 0.0f) atomicAdd(op + kCols * s + 1, v.y);
+      for (int s = 0; s < SW; ++s) {
+        const float2 v = __fmul2_rn(cache[rs][s], inv2);
+        if (v.x != 0.0f) atomicAdd(op + kCols * s, v.x);
+        if (v.y != 0.0f) atomicAdd(op + kCols * s + 1, v.y);
+      }
+    }
+  } else {
+    // q = floor(v 2^22 + U), U uniform in [0, 1) per event: E[q] = v 2^22
+    const float dither =
+        static_cast<float>(hash32(dither_key) >> 8) * 5.9604644775390625e-08f - 0.5f;
+    const float sc = inv * kFixedScale;
+    const float2 sc2 = make_float2(sc, sc), d2 = make_float2(dither, dither);
+    const float2 m2 = make_float2(kMagic, kMagic);
+    uint32_t* oq = reinterpret_cast<uint32_t*>(w_out);
+#pragma unroll
+    for (int rs = 0; rs < RS; ++rs) {
+      const int src = (rs * kRPS) % 32 + gid;
+      const int set = (rs * kRPS) / 32;
+      const int base = __shfl_sync(kFull, rb[set], src);
+      uint32_t* op = oq + base + 2 * gl;
+#pragma unroll
+      for (int s = 0; s < SW; ++s) {
+        const float2 x = __fadd2_rn(__ffma2_rn(cache[rs][s], sc2, d2), m2);
+        const uint32_t q0 = __float_as_uint(x.x) - 0x4B400000u;
+        const uint32_t q1 = __float_as_uint(x.y) - 0x4B400000u;
+        if (q0 != 0u) atomicAdd(op + kCols * s, q0);
+        if (q1 != 0u) atomicAdd(op + kCols * s + 1, q1);
+      }
     }
   }
   return true;
 }
 
-template <int RS, int SW>
+template <int RS, int SW, int ACC, bool DEN64>
 __global__ void __launch_bounds__(256) iterate_fast_kernel(
     DevGeom g, FastConst fc, Tiling t, const Chunk* __restrict__ chunks,
     const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
     const uint16_t* __restrict__ rows, const float* __restrict__ rho, float* __restrict__ out,
-    DevCounters* counters) {
+    double* __restrict__ out64, DevCounters* counters, uint32_t seed) {
   extern __shared__ __align__(16) float smem[];
   const int pitch = fast_pitch(t);
   const int wfl = fast_window_floats(t);
@@ -315,14 +371,23 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
     }
     maxw = __reduce_max_sync(kFull, maxw);
     bool ok;
+    const uint32_t key = hash32(static_cast<uint32_t>(ei) ^ seed);
     if (nrows > RS * kRPS || maxw + 1 > SW * kCols) {
-      process_event<kCpuReference>(g, 32, ev, box, acc, nullptr, dummy_calls, contrib);
+      // boxes outside the register-cache shape: reference-order rasteriser;
+      // in the fixed-point mode it adds to the global float image directly
+      if (ACC == kAccFloat) {
+        process_event<kCpuReference>(g, 32, ev, box, acc, nullptr, dummy_calls, contrib);
+      } else {
+        GlobalAccess gacc{rho, out, g.n_z};
+        process_event<kCpuReference>(g, 32, ev, box, gacc, nullptr, dummy_calls, contrib);
+      }
       continue;
     } else if (RS > 4 && nrows <= (RS / 2) * kRPS) {
-      ok = fast_event<(RS > 4 ? RS / 2 : RS), SW>(g, fc, ev, box, ent, nrows, ox, c.oy, pitch,
-                                                  w_rho, w_out, fl);
+      ok = fast_event<(RS > 4 ? RS / 2 : RS), SW, ACC, DEN64>(g, fc, ev, box, ent, nrows, ox, c.oy,
+                                                              pitch, w_rho, w_out, fl, key);
     } else {
-      ok = fast_event<RS, SW>(g, fc, ev, box, ent, nrows, ox, c.oy, pitch, w_rho, w_out, fl);
+      ok = fast_event<RS, SW, ACC, DEN64>(g, fc, ev, box, ent, nrows, ox, c.oy, pitch, w_rho,
+                                          w_out, fl, key);
     }
     if (ok && lane == 0) ++contrib;
   }
@@ -332,25 +397,61 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
     const int gy = c.oy + r;
     for (int col = lane; col < pitch; col += 32) {
       const int gx = ox + col;
-      const float v = w_out[r * pitch + col];
-      if (v != 0.0f && gy < g.n_y && gx < g.n_z) atomicAdd(&out[gy * g.n_z + gx], v);
+      if (ACC == kAccFloat) {
+        const float v = w_out[r * pitch + col];
+        if (v != 0.0f && gy < g.n_y && gx < g.n_z) atomicAdd(&out[gy * g.n_z + gx], v);
+      } else {
+        const uint32_t q = reinterpret_cast<const uint32_t*>(w_out)[r * pitch + col];
+        if (q != 0u && gy < g.n_y && gx < g.n_z)
+          atomicAdd(&out64[gy * g.n_z + gx], static_cast<double>(q) * (1.0 / 4194304.0));
+      }
     }
   }
+}
+
+template <int RS, int SW, int ACC, bool DEN64>
+cudaError_t launch_fast_kernel(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                               const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
+                               const short4* ev_box, const uint16_t* rows, const float* rho,
+                               float* out, double* out64, DevCounters* counters, uint32_t seed,
+                               cudaStream_t s) {
+  const size_t smem = 2ull * fast_window_floats(t) * sizeof(float);
+  cudaError_t err = cudaFuncSetAttribute(iterate_fast_kernel<RS, SW, ACC, DEN64>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+  if (err != cudaSuccess) return err;
+  iterate_fast_kernel<RS, SW, ACC, DEN64><<<n_chunks, t.threads, smem, s>>>(
+      g, fc, t, chunks, ev_geom, ev_box, rows, rho, out, out64, counters, seed);
+  return cudaGetLastError();
 }
 
 template <int RS, int SW>
 cudaError_t launch_fast_shape(const DevGeom& g, const FastConst& fc, const Tiling& t,
                               const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                               const short4* ev_box, const uint16_t* rows, const float* rho,
-                              float* out, DevCounters* counters, cudaStream_t s) {
-  const size_t smem = 2ull * fast_window_floats(t) * sizeof(float);
-  cudaError_t err = cudaFuncSetAttribute(iterate_fast_kernel<RS, SW>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-  if (err != cudaSuccess) return err;
-  iterate_fast_kernel<RS, SW><<<n_chunks, t.threads, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box,
-                                                                rows, rho, out, counters);
-  return cudaGetLastError();
+                              float* out, double* out64, DevCounters* counters, int precision,
+                              uint32_t seed, cudaStream_t s) {
+  switch (precision) {
+    case kPrecisionFixed:
+      return launch_fast_kernel<RS, SW, kAccFixed, false>(g, fc, t, chunks, n_chunks, ev_geom,
+                                                          ev_box, rows, rho, out, out64, counters,
+                                                          seed, s);
+    case kPrecisionFixedDen64:
+      return launch_fast_kernel<RS, SW, kAccFixed, true>(g, fc, t, chunks, n_chunks, ev_geom,
+                                                         ev_box, rows, rho, out, out64, counters,
+                                                         seed, s);
+    default:
+      return launch_fast_kernel<RS, SW, kAccFloat, false>(g, fc, t, chunks, n_chunks, ev_geom,
+                                                          ev_box, rows, rho, out, out64, counters,
+                                                          seed, s);
+  }
+}
+
+__global__ void combine_fixed_kernel(const double* __restrict__ out64,
+                                     const float* __restrict__ out_f, float* __restrict__ rho,
+                                     int64_t n) {
+  int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) rho[i] = static_cast<float>(out64[i] + static_cast<double>(out_f[i]));
 }
 
 }  // namespace
@@ -369,19 +470,28 @@ cudaError_t launch_row_tables(const DevGeom& g, const Tiling& t, int32_t n_event
 cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint16_t* rows, const float* rho,
-                                float* out, DevCounters* counters, cudaStream_t s) {
+                                float* out, double* out64, DevCounters* counters, int precision,
+                                uint32_t seed, cudaStream_t s) {
   if (n_chunks <= 0) return cudaSuccess;
   switch (t.fast_shape) {
     case kShapeS:
       return launch_fast_shape<4, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out,
-                                     counters, s);
+                                     out64, counters, precision, seed, s);
     case kShapeM:
       return launch_fast_shape<8, 3>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out,
-                                     counters, s);
+                                     out64, counters, precision, seed, s);
     default:
       return launch_fast_shape<12, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho,
-                                      out, counters, s);
+                                      out, out64, counters, precision, seed, s);
   }
+}
+
+cudaError_t launch_combine_fixed(const double* out64, const float* out_f, float* rho, int64_t n,
+                                 cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  combine_fixed_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(out64, out_f, rho,
+                                                                             n);
+  return cudaGetLastError();
 }
 
 }  // namespace jpet

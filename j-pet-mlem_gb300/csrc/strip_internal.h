@@ -87,10 +87,17 @@ cudaError_t launch_fill(float* p, float v, int64_t n, cudaStream_t s);
 cudaError_t launch_row_tables(const DevGeom& g, const Tiling& t, int32_t n_events,
                               const float4* ev_geom, const short4* ev_box, uint16_t* rows,
                               unsigned long long* kernel_calls, cudaStream_t s);
+// Accumulation of the fast kernel: float shared atomics, or exact fixed-point
+// tile sums flushed into an FP64 image (optionally with FP64 denominators).
+enum FastPrecision : int32_t { kPrecisionFloat = 0, kPrecisionFixed = 1, kPrecisionFixedDen64 = 2 };
 cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint16_t* rows, const float* rho,
-                                float* out, DevCounters* counters, cudaStream_t s);
+                                float* out, double* out64, DevCounters* counters, int precision,
+                                uint32_t seed, cudaStream_t s);
+// rho = float(out64 + out_f)
+cudaError_t launch_combine_fixed(const double* out64, const float* out_f, float* rho, int64_t n,
+                                 cudaStream_t s);
 cudaError_t launch_iterate(const DevGeom& g, const Tiling& t, int32_t semantics,
                            const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                            const short4* ev_box, const float* rho, const float* sens,

@@ -29,7 +29,7 @@ JPET_ERR_UNSUPPORTED = -6
 MODE_CPU_REFERENCE = 0
 MODE_GPU_REFERENCE = 1
 PRECISION_FP32 = 0
-PRECISION_KAHAN = 1
+PRECISION_COMPENSATED = 1
 PRECISION_FP64_DEN = 2
 VARIANT_FAST = 0
 VARIANT_EXACT = 1

@@ -1,0 +1,90 @@
+"""The host command-line tool 2d_strip_reconstruction: the reference's options,
+input formats and output naming (src/2d/strip/reconstruction_cmd.cpp:105-301)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+TOOL = os.path.join(ROOT, "j-pet-mlem_gb300", "bin", "2d_strip_reconstruction")
+
+pytestmark = pytest.mark.skipif(not os.path.exists(TOOL), reason="host tool not built")
+
+GEOM = ["-r", "450", "-l", "1000", "-p", "5", "--n-z-pixels", "200", "--n-y-pixels", "180",
+        "--s-z", "10", "--s-dl", "42"]
+
+
+def run(args, cwd=None):
+    return subprocess.run([TOOL] + args, capture_output=True, text=True, cwd=cwd, timeout=300)
+
+
+def test_usage_without_arguments():
+    r = run([])
+    assert r.returncode == 0
+    for opt in ["--radius", "--length", "--s-pixel", "--n-z-pixels", "--n-y-pixels", "--s-z",
+                "--s-dl", "--blocks", "--iterations", "--output", "--gpu", "--cuda-device",
+                "--rho", "--rho-is-int", "--3d-response", "--dl-is-time", "--scale-length"]:
+        assert opt in r.stderr
+
+
+def test_missing_input_and_bad_option():
+    r = run(["-i", "1"])
+    assert r.returncode == 1 and "at least one responses input file expected" in r.stderr
+    r = run(["--no-such-option", "x.bin"])
+    assert r.returncode == 1 and "undefined option" in r.stderr
+    r = run(["-i", "abc", "x.bin"])
+    assert r.returncode == 1 and "option value is invalid" in r.stderr
+
+
+@pytest.mark.gpu
+def test_binary_input_matches_reference_golden(tmp_path, golden):
+    manifest, load = golden
+    ev = load("c1_events.npy")
+    ev.tofile(tmp_path / "ev.bin")
+    r = run([str(tmp_path / "ev.bin")] + GEOM + ["-i", "3", "-I", "1", "-o",
+                                                 str(tmp_path / "r.bin")])
+    assert r.returncode == 0, r.stderr
+    for it in (1, 3):
+        got = np.fromfile(tmp_path / f"r_{it}.bin", np.float32).reshape(180, 200)
+        want = load(f"c1_strict_it{it:02d}.npy")
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-5
+        nrrd = (tmp_path / f"r_{it}.nrrd").read_text()
+        assert "sizes: 200 180" in nrrd and f"data file: ./r_{it}.bin" in nrrd
+
+
+@pytest.mark.gpu
+def test_text_input_and_tuples_output(tmp_path, golden):
+    import oracle as O
+
+    manifest, load = golden
+    ev = load("c1_events.npy")[:3000]
+    with open(tmp_path / "ev.txt", "w") as f:
+        for zu, zd, dl in ev:
+            f.write(f"{zu:.6f} {zd:.6f} {dl:.6f}\n")
+    r = run([str(tmp_path / "ev.txt")] + GEOM + ["-i", "1", "-I", "2", "-o",
+                                                 str(tmp_path / "t.txt")])
+    assert r.returncode == 0, r.stderr
+    lines = (tmp_path / "t_2.txt").read_text().split("\n")
+    got = np.zeros((180, 200), np.float64)
+    for ln in lines:
+        if ln.strip():
+            x, y, v = ln.split()
+            got[int(y), int(x)] = float(v)
+    parsed = np.loadtxt(tmp_path / "ev.txt", dtype=np.float64).astype(np.float32)
+    want, _ = O.mlem_f(O.Geometry(450, 1000, 180, 200, 5, 10, 42), parsed, 2, threads=4)
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-5
+
+
+@pytest.mark.gpu
+def test_gpu_mode_output_protocol(tmp_path, golden):
+    manifest, load = golden
+    ev = load("c1_events.npy")[:2000]
+    ev.tofile(tmp_path / "ev.bin")
+    r = run([str(tmp_path / "ev.bin")] + GEOM + ["-i", "2", "-I", "3", "--gpu", "-v", "-o",
+                                                 str(tmp_path / "g.bin")])
+    assert r.returncode == 0, r.stderr
+    names = sorted(p.name for p in tmp_path.iterdir() if p.suffix == ".bin" and p.name != "ev.bin")
+    # sensitivity, iterations 1..3 of block 0 (i < I-1 and the block end), block end 6
+    assert names == ["g_1.bin", "g_2.bin", "g_3.bin", "g_6.bin", "g_sensitivity.bin"]
+    assert "# device:" in r.stderr

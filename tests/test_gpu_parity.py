@@ -246,3 +246,43 @@ def test_fast_kernel_register_shapes(sigma):
     want, st = O.mlem_f(og, ev, 2, threads=8)
     assert rel_l2(got, want) < TOL_ITER
     assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_COMPENSATED, capi.PRECISION_FP64_DEN])
+def test_compensated_precision_modes(golden, precision):
+    manifest, load = golden
+    cg, og = _geoms(manifest["c1"])
+    ev = load("c1_events.npy")
+    f64 = load("c1_fp64_it03.npy")
+    with capi.StripReconstruction(cg, precision=precision) as rec:
+        rec.set_events(ev)
+        rho = None
+        for it in range(3):
+            rec.iterate(1)
+            rho, st = O.mlem_f(og, ev, 1, rho, threads=4)
+            assert rel_l2(rec.rho, rho) < TOL_ITER
+            cnt = rec.counters()
+            assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
+            assert cnt["n_contributing"] == st["n_contributing"]
+            rec.rho = rho
+    with capi.StripReconstruction(cg, precision=precision) as rec, \
+            capi.StripReconstruction(cg) as plain:
+        rec.set_events(ev)
+        plain.set_events(ev)
+        rec.iterate(3)
+        plain.iterate(3)
+        e_comp = rel_l2(rec.rho, f64)
+        e_plain = rel_l2(plain.rho, f64)
+    # error against the FP64 reference template is not worse than plain FP32
+    assert e_comp < max(2.0 * e_plain, 1e-6), (e_comp, e_plain)
+
+
+def test_precision_mode_argument_checks():
+    g = capi.Geometry(450, 1000, 90, 100, 10, 10, 42)
+    with pytest.raises(capi.StripError) as e:
+        capi.StripReconstruction(g, precision=7)
+    assert e.value.code == capi.JPET_ERR_ARGUMENT
+    with pytest.raises(capi.StripError) as e:
+        capi.StripReconstruction(g, precision=capi.PRECISION_COMPENSATED,
+                                 variant=capi.VARIANT_EXACT)
+    assert e.value.code == capi.JPET_ERR_UNSUPPORTED
