@@ -56,7 +56,8 @@ def parse():
     p.add_argument("--no-peaks", action="store_true", help="skip the peak microbenchmarks")
     p.add_argument("--variant", type=int, default=0, help="0 fast kernel, 1 exact kernel")
     p.add_argument("--precision", type=int, default=0,
-                   help="0 FP32 tile sums, 1 compensated (exact) tile sums, 2 plus FP64 denominators")
+                   help="0 FP32 tile sums, 1 compensated tile sums, 2 plus FP64 denominators, "
+                        "3 fixed-point tile sums")
     return p.parse_args()
 
 
@@ -323,7 +324,7 @@ def gb300_arm(args, wl, world, rank, local):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "kernel": {"variant": ["fast", "exact"][args.variant],
-                   "precision": ["fp32", "compensated", "fp64_den"][args.precision]},
+                   "precision": ["fp32", "compensated", "fp64_den", "fixed"][args.precision]},
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl.name, "events": n_events, "grid": f"{wl.n_z}x{wl.n_y}",

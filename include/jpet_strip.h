@@ -64,14 +64,15 @@ typedef struct jpet_strip_geom {
 /* accumulation precision (fast kernel; the exact kernel and the GPU-reference
  * mode accumulate in FP32) */
 #define JPET_PRECISION_FP32 0        /* FP32 evaluation, FP32 shared-memory tile sums, FP32 image */
-#define JPET_PRECISION_COMPENSATED 1 /* FP32 evaluation; per-tile sums are error-free: each
-                                        contribution is rounded once to 2^-22 of an event
-                                        (unbiased dither) and summed in integers, tiles are
-                                        added into an FP64 image.  This plays the role of a
-                                        Kahan correction, which shared-memory atomics cannot
-                                        carry, and is independent of the summation order */
+#define JPET_PRECISION_COMPENSATED 1 /* FP32 evaluation; every shared-memory tile addition
+                                        also adds its exact rounding error (TwoSum) to a
+                                        compensation tile; tile sum + compensation go into
+                                        an FP64 image (compensated, Kahan-style, per tile) */
 #define JPET_PRECISION_FP64_DEN 2    /* as COMPENSATED, plus per-event denominators reduced
                                         in FP64 */
+#define JPET_PRECISION_FIXED 3       /* deterministic tiles: each contribution rounded once to
+                                        2^-22 of an event (unbiased per-event dither) and
+                                        summed with integer shared atomics; FP64 image */
 
 /* iteration kernel */
 #define JPET_VARIANT_FAST 0  /* exp2-form kernel, packed f32x2, register-cached K*rho (default) */
@@ -168,6 +169,22 @@ int jpet_strip_get_counters(jpet_strip_t* h, jpet_strip_counters* out);
 
 /* Synchronises the handle's stream and reports any asynchronous error. */
 int jpet_strip_synchronize(jpet_strip_t* h);
+
+/* Poisson list-mode negative log-likelihood of the current events and its
+ * gradients (no counterpart in the reference, which has no likelihood code):
+ *   L = sum_p s_p rho_p - sum_e log(sum_{p in E_e} K_e(p; sigma) rho_p)
+ * with the reference's Gaussian kernel including its normalisation
+ * (gaussian_kernel.h:27-79) at the kernel widths (sigma_z, sigma_dl), and the
+ * support E_e = the event's 3-sigma ellipse for the handle's own widths, held
+ * fixed.  d_rho: device float[n_y*n_z] (NULL = the current image); d_sens: device
+ * sensitivity s (NULL = point sensitivity, kind 0); d_grad_rho: device
+ * float[n_y*n_z] receiving dL/drho, or NULL.  loss, grad_sigma[2] (dL/dsigma_z,
+ * dL/dsigma_dl) and n_skipped (events with a zero denominator, left out) are
+ * host pointers, each may be NULL.  Synchronises the stream.  Needs the
+ * CPU-reference mode. */
+int jpet_strip_nll_grad(jpet_strip_t* h, double sigma_z, double sigma_dl, const float* d_rho,
+                        const float* d_sens, double* loss, float* d_grad_rho,
+                        double* grad_sigma, int64_t* n_skipped);
 
 /* The full reference GPU entry point over host buffers: uploads the events,
  * starts from rho (in/out, float[n_y*n_z]), runs n_blocks * n_iterations_in_block

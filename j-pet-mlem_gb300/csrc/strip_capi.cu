@@ -73,6 +73,8 @@ struct jpet_strip {
   bool counters_valid = false;
   unsigned long long table_kernel_calls = 0;
   DevBuf<unsigned long long> box_pixels;
+  DevBuf<double> nll_acc;            // loss, d/dsigma_z, d/dsigma_dl
+  DevBuf<float> nll_grad_tmp;        // gradient image when the caller passes none
   DevBuf<DevCounters> counters;
 
   int64_t n_events = 0;
@@ -403,7 +405,7 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
     return JPET_ERR_ARGUMENT;
   }
   if (o.precision != JPET_PRECISION_FP32 && o.precision != JPET_PRECISION_COMPENSATED &&
-      o.precision != JPET_PRECISION_FP64_DEN) {
+      o.precision != JPET_PRECISION_FP64_DEN && o.precision != JPET_PRECISION_FIXED) {
     g_create_error = "unknown precision mode";
     return JPET_ERR_ARGUMENT;
   }
@@ -494,6 +496,8 @@ int jpet_strip_destroy(jpet_strip_t* h) {
   h->chunks.release();
   h->row_table.release();
   h->box_pixels.release();
+  h->nll_acc.release();
+  h->nll_grad_tmp.release();
   h->counters.release();
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
@@ -571,9 +575,10 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
     if (fixed)
       JPET_CUDA(h, cudaMemsetAsync(h->out64.p, 0, n_pix * sizeof(double), s), "clear image");
     if (h->use_fast) {
-      const int prec = h->opts.precision == JPET_PRECISION_COMPENSATED ? kPrecisionFixed
-                       : h->opts.precision == JPET_PRECISION_FP64_DEN  ? kPrecisionFixedDen64
-                                                                       : kPrecisionFloat;
+      const int prec = h->opts.precision == JPET_PRECISION_COMPENSATED ? kPrecisionCompensated
+                       : h->opts.precision == JPET_PRECISION_FP64_DEN ? kPrecisionCompensatedDen64
+                       : h->opts.precision == JPET_PRECISION_FIXED    ? kPrecisionFixed
+                                                                      : kPrecisionFloat;
       const uint32_t seed = 0x9E3779B9u * static_cast<uint32_t>(h->iterations_done + 1);
       JPET_CUDA(h, launch_iterate_fast(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
                                        h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
@@ -652,6 +657,51 @@ int jpet_strip_synchronize(jpet_strip_t* h) {
   if (!h) return JPET_ERR_ARGUMENT;
   JPET_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
   JPET_CUDA(h, cudaStreamSynchronize(h->stream), "stream");
+  return JPET_OK;
+}
+
+int jpet_strip_nll_grad(jpet_strip_t* h, double sigma_z, double sigma_dl, const float* d_rho,
+                        const float* d_sens, double* loss, float* d_grad_rho,
+                        double* grad_sigma, int64_t* n_skipped) {
+  if (!h) return JPET_ERR_ARGUMENT;
+  if (!(sigma_z > 0) || !(sigma_dl > 0))
+    return h->fail(JPET_ERR_ARGUMENT, "kernel sigmas must be positive");
+  if (!h->events_ready) return h->fail(JPET_ERR_STATE, "set_events has not succeeded");
+  if (h->opts.mode != JPET_MODE_CPU_REFERENCE)
+    return h->fail(JPET_ERR_UNSUPPORTED, "the likelihood uses the Gaussian kernel (CPU-reference mode)");
+  JPET_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t s = h->stream;
+  const size_t n_pix = static_cast<size_t>(h->g.n_y) * h->g.n_z;
+  JPET_CUDA(h, h->nll_acc.alloc(4), "cudaMalloc(likelihood)");
+  float* grad = d_grad_rho;
+  if (!grad) {
+    JPET_CUDA(h, h->nll_grad_tmp.alloc(n_pix), "cudaMalloc(gradient)");
+    grad = h->nll_grad_tmp.p;
+  }
+  const float* rho = d_rho ? d_rho : h->rho.p;
+  const float* sens = d_sens ? d_sens : h->sens_point.p;
+  JPET_CUDA(h, cudaMemsetAsync(h->nll_acc.p, 0, 4 * sizeof(double), s), "memset");
+  JPET_CUDA(h, cudaMemsetAsync(grad, 0, n_pix * sizeof(float), s), "memset");
+  const NllConst k = make_nll_const(sigma_z, sigma_dl);
+  JPET_CUDA(h, launch_nll_grad(h->g, k, h->tiling, h->chunks.p, h->n_chunks, h->sorted_geom.p,
+                               h->sorted_box.p, h->n_oversize, h->over_geom.p, h->over_box.p, rho,
+                               grad, h->nll_acc.p,
+                               reinterpret_cast<unsigned long long*>(h->nll_acc.p + 3), s),
+            "likelihood kernel launch");
+  JPET_CUDA(h, launch_nll_finish(sens, rho, grad, h->nll_acc.p, static_cast<int64_t>(n_pix), s),
+            "likelihood finish launch");
+  double host[4];
+  JPET_CUDA(h, cudaMemcpyAsync(host, h->nll_acc.p, sizeof(host), cudaMemcpyDeviceToHost, s),
+            "copy likelihood");
+  JPET_CUDA(h, cudaStreamSynchronize(s), "likelihood");
+  if (loss) *loss = host[0];
+  if (grad_sigma) {
+    grad_sigma[0] = host[1];
+    grad_sigma[1] = host[2];
+  }
+  unsigned long long sk;
+  std::memcpy(&sk, &host[3], sizeof(sk));
+  if (n_skipped) *n_skipped = static_cast<int64_t>(sk);
   return JPET_OK;
 }
 

@@ -159,6 +159,52 @@ __device__ __forceinline__ float analytic_exact(const DevGeom& g, float y, float
   return __fmul_rn(ebe, expf(arg));
 }
 
+// Exact column interval of box row iy whose pixel centres pass the reference's
+// 3-sigma test (in_ellipse above, reference rounding).  The test's quadratic is
+// convex along the row, so the passing columns form one interval; it is found
+// from the analytic endpoints tan*dy +- sqrt((9 - 4 ipd sec^2 dy^2)/(2 ipz)) and
+// corrected by evaluating the exact test around them.  Every loop is bounded by
+// the box.  Returns the width (0 if no pixel passes) and the first column.
+__device__ __forceinline__ int row_interval(const DevGeom& g, float A, float B, float C, float z,
+                                            float y, float t, float sec, int bx, int bz, int iy,
+                                            int& first) {
+  const float dy = __fsub_rn(pixel_center_y(g, iy), y);
+  auto pass = [&](int c) { return in_ellipse(A, B, C, dy, __fsub_rn(pixel_center_z(g, c), z)); };
+  const float inv_pw = 1.0f / g.pixel_width;
+  const float h =
+      sqrtf(fmaxf((9.0f - 4.0f * sec * sec * g.ipd * dy * dy) * (0.5f / g.ipz), 0.0f)) * inv_pw;
+  const float xc = (z + t * dy - g.tl_z_half_w) * inv_pw;
+  const float fbx = static_cast<float>(bx), fbz = static_cast<float>(bz - 1);
+  first = bx;
+  if (bz <= bx) return 0;
+  // the column nearest the minimum of the convex test quadratic
+  int cs = static_cast<int>(fminf(fmaxf(rintf(xc), fbx), fbz));
+  bool any = pass(cs);
+  if (!any && cs - 1 >= bx && pass(cs - 1)) {
+    cs -= 1;
+    any = true;
+  }
+  if (!any && cs + 1 < bz && pass(cs + 1)) {
+    cs += 1;
+    any = true;
+  }
+  if (!any) return 0;
+  int lo = static_cast<int>(fminf(fmaxf(ceilf(xc - h), fbx), static_cast<float>(cs)));
+  if (pass(lo)) {
+    while (lo > bx && pass(lo - 1)) --lo;
+  } else {
+    while (lo < cs && !pass(lo)) ++lo;
+  }
+  int hi = static_cast<int>(fminf(fmaxf(floorf(xc + h), static_cast<float>(cs)), fbz));
+  if (pass(hi)) {
+    while (hi < bz - 1 && pass(hi + 1)) ++hi;
+  } else {
+    while (hi > cs && !pass(hi)) --hi;
+  }
+  first = lo;
+  return hi - lo + 1;
+}
+
 // Scanner::sensitivity (scanner.h:147-171), float.
 __device__ __forceinline__ float scanner_sensitivity(const DevGeom& g, float px, float py) {
   float half = g.half_length;

@@ -76,46 +76,11 @@ __global__ void __launch_bounds__(256) row_table_kernel(DevGeom g, int32_t n, in
     const float z = ev.x, y = ev.y, t = ev.z, sec = ev.w;
     float A, B, C;
     ellipse_abc(g, t, sec, A, B, C);
-    const float sec2_ipd4 = 4.0f * sec * sec * g.ipd;
-    const float inv_2ipz = 0.5f / g.ipz;
-    const float inv_pw = 1.0f / g.pixel_width;
     const int nrows = b.w - b.y;
     const int bx = b.x, bz = b.z;
     for (int ri = lane; ri < nrows; ri += 32) {
-      const int iy = b.y + ri;
-      const float dy = __fsub_rn(pixel_center_y(g, iy), y);
-      auto pass = [&](int c) { return in_ellipse(A, B, C, dy, __fsub_rn(pixel_center_z(g, c), z)); };
-      const float h = sqrtf(fmaxf((9.0f - sec2_ipd4 * dy * dy) * inv_2ipz, 0.0f)) * inv_pw;
-      const float xc = (z + t * dy - g.tl_z_half_w) * inv_pw;
-      const float fbx = static_cast<float>(bx), fbz = static_cast<float>(bz - 1);
-      // the column nearest the minimum of the convex test quadratic
-      int cs = static_cast<int>(fminf(fmaxf(rintf(xc), fbx), fbz));
-      bool any = pass(cs);
-      if (!any && cs - 1 >= bx && pass(cs - 1)) {
-        cs -= 1;
-        any = true;
-      }
-      if (!any && cs + 1 < bz && pass(cs + 1)) {
-        cs += 1;
-        any = true;
-      }
-      int w = 0, first = bx;
-      if (any) {
-        int lo = static_cast<int>(fminf(fmaxf(ceilf(xc - h), fbx), static_cast<float>(cs)));
-        if (pass(lo)) {
-          while (lo > bx && pass(lo - 1)) --lo;
-        } else {
-          while (lo < cs && !pass(lo)) ++lo;
-        }
-        int hi = static_cast<int>(fminf(fmaxf(floorf(xc + h), static_cast<float>(cs)), fbz));
-        if (pass(hi)) {
-          while (hi < bz - 1 && pass(hi + 1)) ++hi;
-        } else {
-          while (hi > cs && !pass(hi)) --hi;
-        }
-        first = lo;
-        w = hi - lo + 1;
-      }
+      int first;
+      const int w = row_interval(g, A, B, C, z, y, t, sec, bx, bz, b.y + ri, first);
       rows[static_cast<size_t>(e) * stride + ri] =
           static_cast<uint16_t>((first - bx) | (w << 8));
       calls += static_cast<unsigned long long>(w);
@@ -153,12 +118,17 @@ struct FastLane {
 
 // Accumulation of the back-projection window.
 //   kAccFloat: float shared-memory atomics (red.shared.add.f32)
+//   kAccCompensated: float shared atomics that return the old value; the exact
+//              rounding error of every addition (Knuth's TwoSum) is added to a
+//              second, compensation window, so sum + compensation carries the
+//              tile total to second order (the compensated-summation idea of
+//              Kahan and Neumaier, made atomic); tiles go to an FP64 image.
 //   kAccFixed: each contribution (a fraction of one event, in [0, 1]) rounded to
 //              22 fractional bits with an unbiased per-event dither and added
 //              with integer shared atomics; a window pixel of a chunk of <= 512
-//              events then stays below 2^31, and its sum is exact and
-//              independent of the order of the additions.
-enum Acc : int { kAccFloat = 0, kAccFixed = 1 };
+//              events then stays below 2^31, and its sum is independent of the
+//              order of the additions (deterministic tiles).
+enum Acc : int { kAccFloat = 0, kAccCompensated = 1, kAccFixed = 2 };
 constexpr float kFixedScale = 4194304.0f;     // 2^22
 constexpr float kMagic = 12582912.0f;         // 1.5 * 2^23: float -> integer rounding
 
@@ -182,7 +152,8 @@ template <int RS, int SW, int ACC, bool DEN64>
 __device__ __forceinline__ bool fast_event(const DevGeom& g, const FastConst& fc, float4 ev,
                                            short4 box, const uint32_t* ent, int nrows, int ox,
                                            int oy, int pitch, const float* w_rho, float* w_out,
-                                           const FastLane& fl, uint32_t dither_key) {
+                                           float* w_comp, const FastLane& fl,
+                                           uint32_t dither_key) {
   constexpr int kSets = (RS * kRPS + 31) / 32;
   const int lane = threadIdx.x & 31;
   const int gid = lane / kG, gl = lane % kG;
@@ -278,6 +249,31 @@ __device__ __forceinline__ bool fast_event(const DevGeom& g, const FastConst& fc
         if (v.y != 0.0f) atomicAdd(op + kCols * s + 1, v.y);
       }
     }
+  } else if (ACC == kAccCompensated) {
+    const float2 inv2 = make_float2(inv, inv);
+#pragma unroll
+    for (int rs = 0; rs < RS; ++rs) {
+      const int src = (rs * kRPS) % 32 + gid;
+      const int set = (rs * kRPS) / 32;
+      const int base = __shfl_sync(kFull, rb[set], src) + 2 * gl;
+#pragma unroll
+      for (int s = 0; s < SW; ++s) {
+        const float2 v = __fmul2_rn(cache[rs][s], inv2);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const float x = h ? v.y : v.x;
+          if (x != 0.0f) {
+            const int i = base + kCols * s + h;
+            const float old = atomicAdd(w_out + i, x);
+            // TwoSum: old + x = t + err exactly, t the value now in memory
+            const float t = __fadd_rn(old, x);
+            const float bp = __fsub_rn(t, old);
+            const float err = __fadd_rn(__fsub_rn(old, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+            if (err != 0.0f) atomicAdd(w_comp + i, err);
+          }
+        }
+      }
+    }
   } else {
     // q = floor(v 2^22 + U), U uniform in [0, 1) per event: E[q] = v 2^22
     const float dither =
@@ -316,6 +312,7 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
   const int wfl = fast_window_floats(t);
   float* w_rho = smem;
   float* w_out = smem + wfl;
+  float* w_comp = (ACC == kAccCompensated) ? smem + 2 * wfl : nullptr;
   const Chunk c = chunks[blockIdx.x];
   const int ox = c.ox & ~1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
@@ -325,6 +322,7 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
       const int gx = ox + col;
       w_rho[r * pitch + col] = (gy < g.n_y && gx < g.n_z) ? rho[gy * g.n_z + gx] : 0.0f;
       w_out[r * pitch + col] = 0.0f;
+      if (ACC == kAccCompensated) w_comp[r * pitch + col] = 0.0f;
     }
   }
   for (int i = threadIdx.x; i < 64; i += blockDim.x) w_rho[t.win_h * pitch + i] = 0.0f;
@@ -383,11 +381,11 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
       }
       continue;
     } else if (RS > 4 && nrows <= (RS / 2) * kRPS) {
-      ok = fast_event<(RS > 4 ? RS / 2 : RS), SW, ACC, DEN64>(g, fc, ev, box, ent, nrows, ox, c.oy,
-                                                              pitch, w_rho, w_out, fl, key);
+      ok = fast_event<(RS > 4 ? RS / 2 : RS), SW, ACC, DEN64>(
+          g, fc, ev, box, ent, nrows, ox, c.oy, pitch, w_rho, w_out, w_comp, fl, key);
     } else {
       ok = fast_event<RS, SW, ACC, DEN64>(g, fc, ev, box, ent, nrows, ox, c.oy, pitch, w_rho,
-                                          w_out, fl, key);
+                                          w_out, w_comp, fl, key);
     }
     if (ok && lane == 0) ++contrib;
   }
@@ -400,6 +398,10 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
       if (ACC == kAccFloat) {
         const float v = w_out[r * pitch + col];
         if (v != 0.0f && gy < g.n_y && gx < g.n_z) atomicAdd(&out[gy * g.n_z + gx], v);
+      } else if (ACC == kAccCompensated) {
+        const float v = w_out[r * pitch + col], cv = w_comp[r * pitch + col];
+        if ((v != 0.0f || cv != 0.0f) && gy < g.n_y && gx < g.n_z)
+          atomicAdd(&out64[gy * g.n_z + gx], static_cast<double>(v) + static_cast<double>(cv));
       } else {
         const uint32_t q = reinterpret_cast<const uint32_t*>(w_out)[r * pitch + col];
         if (q != 0u && gy < g.n_y && gx < g.n_z)
@@ -415,7 +417,8 @@ cudaError_t launch_fast_kernel(const DevGeom& g, const FastConst& fc, const Tili
                                const short4* ev_box, const uint16_t* rows, const float* rho,
                                float* out, double* out64, DevCounters* counters, uint32_t seed,
                                cudaStream_t s) {
-  const size_t smem = 2ull * fast_window_floats(t) * sizeof(float);
+  const size_t smem =
+      (ACC == kAccCompensated ? 3ull : 2ull) * fast_window_floats(t) * sizeof(float);
   cudaError_t err = cudaFuncSetAttribute(iterate_fast_kernel<RS, SW, ACC, DEN64>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
@@ -432,14 +435,16 @@ cudaError_t launch_fast_shape(const DevGeom& g, const FastConst& fc, const Tilin
                               float* out, double* out64, DevCounters* counters, int precision,
                               uint32_t seed, cudaStream_t s) {
   switch (precision) {
+    case kPrecisionCompensated:
+      return launch_fast_kernel<RS, SW, kAccCompensated, false>(
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out, out64, counters, seed, s);
+    case kPrecisionCompensatedDen64:
+      return launch_fast_kernel<RS, SW, kAccCompensated, true>(
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out, out64, counters, seed, s);
     case kPrecisionFixed:
       return launch_fast_kernel<RS, SW, kAccFixed, false>(g, fc, t, chunks, n_chunks, ev_geom,
                                                           ev_box, rows, rho, out, out64, counters,
                                                           seed, s);
-    case kPrecisionFixedDen64:
-      return launch_fast_kernel<RS, SW, kAccFixed, true>(g, fc, t, chunks, n_chunks, ev_geom,
-                                                         ev_box, rows, rho, out, out64, counters,
-                                                         seed, s);
     default:
       return launch_fast_kernel<RS, SW, kAccFloat, false>(g, fc, t, chunks, n_chunks, ev_geom,
                                                           ev_box, rows, rho, out, out64, counters,

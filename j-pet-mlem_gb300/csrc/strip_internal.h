@@ -87,14 +87,36 @@ cudaError_t launch_fill(float* p, float v, int64_t n, cudaStream_t s);
 cudaError_t launch_row_tables(const DevGeom& g, const Tiling& t, int32_t n_events,
                               const float4* ev_geom, const short4* ev_box, uint16_t* rows,
                               unsigned long long* kernel_calls, cudaStream_t s);
-// Accumulation of the fast kernel: float shared atomics, or exact fixed-point
-// tile sums flushed into an FP64 image (optionally with FP64 denominators).
-enum FastPrecision : int32_t { kPrecisionFloat = 0, kPrecisionFixed = 1, kPrecisionFixedDen64 = 2 };
+// Accumulation of the fast kernel: float shared atomics; compensated tile sums
+// flushed into an FP64 image (optionally with FP64 denominators); or
+// deterministic fixed-point tile sums flushed into an FP64 image.
+enum FastPrecision : int32_t {
+  kPrecisionFloat = 0,
+  kPrecisionCompensated = 1,
+  kPrecisionCompensatedDen64 = 2,
+  kPrecisionFixed = 3,
+};
 cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint16_t* rows, const float* rho,
                                 float* out, double* out64, DevCounters* counters, int precision,
                                 uint32_t seed, cudaStream_t s);
+// Constants of the likelihood adjoint at the kernel sigmas (strip_adjoint.cu).
+struct NllConst {
+  float ipz, ipd, kz, kdl, inv_ipz, half_inv_ipd, dipz_dsz, dipd_dsdl;
+  double log_c0;
+};
+NllConst make_nll_const(double sigma_z, double sigma_dl);
+// acc[0] -= sum_e log den_e, acc[1..2] -= sum_e (d den_e / d sigma) / den_e,
+// grad -= sum_e K_e / den_e
+cudaError_t launch_nll_grad(const DevGeom& g, const NllConst& k, const Tiling& t,
+                            const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
+                            const short4* ev_box, int32_t n_over, const float4* over_geom,
+                            const short4* over_box, const float* rho, float* grad, double* acc,
+                            unsigned long long* skipped, cudaStream_t s);
+// acc[0] += sum s rho; grad += s (grad may be null)
+cudaError_t launch_nll_finish(const float* sens, const float* rho, float* grad, double* acc,
+                              int64_t n, cudaStream_t s);
 // rho = float(out64 + out_f)
 cudaError_t launch_combine_fixed(const double* out64, const float* out_f, float* rho, int64_t n,
                                  cudaStream_t s);

@@ -31,6 +31,7 @@ MODE_GPU_REFERENCE = 1
 PRECISION_FP32 = 0
 PRECISION_COMPENSATED = 1
 PRECISION_FP64_DEN = 2
+PRECISION_FIXED = 3
 VARIANT_FAST = 0
 VARIANT_EXACT = 1
 
@@ -42,6 +43,7 @@ EXPORTED = [
     "jpet_strip_set_image", "jpet_strip_set_image_device", "jpet_strip_iterate",
     "jpet_strip_get_image", "jpet_strip_image_device", "jpet_strip_get_sensitivity",
     "jpet_strip_get_counters", "jpet_strip_synchronize", "jpet_strip_run",
+    "jpet_strip_nll_grad",
 ]
 
 
@@ -123,6 +125,9 @@ def lib() -> C.CDLL:
         L.jpet_strip_get_sensitivity.argtypes = [vp, C.c_int, vp]
         L.jpet_strip_get_counters.argtypes = [vp, C.POINTER(Counters)]
         L.jpet_strip_synchronize.argtypes = [vp]
+        L.jpet_strip_nll_grad.argtypes = [vp, C.c_double, C.c_double, vp, vp,
+                                          C.POINTER(C.c_double), vp, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_int64)]
         L.jpet_strip_run.argtypes = [C.POINTER(Geom), C.POINTER(Opts), vp, C.c_int64, vp, C.c_int,
                                      C.c_int, OUTPUT_FN, PROGRESS_FN, vp, C.c_char_p, C.c_size_t]
         for name in EXPORTED:
@@ -247,6 +252,17 @@ class StripReconstruction:
 
     def set_stream(self, stream_ptr: int | None):
         _check(lib().jpet_strip_set_stream(self._h, stream_ptr), self._h)
+
+    def nll_grad(self, sigma_z: float, sigma_dl: float, rho_ptr: int | None = None,
+                 sens_ptr: int | None = None, grad_ptr: int | None = None):
+        """Device pointers in, (loss, (dL/dsigma_z, dL/dsigma_dl), n_skipped) out;
+        dL/drho is written to grad_ptr when given."""
+        loss = C.c_double()
+        gs = (C.c_double * 2)()
+        sk = C.c_int64()
+        _check(lib().jpet_strip_nll_grad(self._h, sigma_z, sigma_dl, rho_ptr, sens_ptr,
+                                         C.byref(loss), grad_ptr, gs, C.byref(sk)), self._h)
+        return loss.value, (gs[0], gs[1]), sk.value
 
     def counters(self) -> dict:
         c = Counters()

@@ -248,7 +248,8 @@ def test_fast_kernel_register_shapes(sigma):
     assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
 
 
-@pytest.mark.parametrize("precision", [capi.PRECISION_COMPENSATED, capi.PRECISION_FP64_DEN])
+@pytest.mark.parametrize("precision", [capi.PRECISION_COMPENSATED, capi.PRECISION_FP64_DEN,
+                                       capi.PRECISION_FIXED])
 def test_compensated_precision_modes(golden, precision):
     manifest, load = golden
     cg, og = _geoms(manifest["c1"])
@@ -273,8 +274,12 @@ def test_compensated_precision_modes(golden, precision):
         plain.iterate(3)
         e_comp = rel_l2(rec.rho, f64)
         e_plain = rel_l2(plain.rho, f64)
-    # error against the FP64 reference template is not worse than plain FP32
-    assert e_comp < max(2.0 * e_plain, 1e-6), (e_comp, e_plain)
+    # error against the FP64 reference template: compensated tiles are not worse
+    # than plain FP32; fixed-point tiles are quantized to 2^-22 of an event
+    if precision == capi.PRECISION_FIXED:
+        assert e_comp < 1e-5, e_comp
+    else:
+        assert e_comp <= 1.05 * e_plain + 1e-9, (e_comp, e_plain)
 
 
 def test_precision_mode_argument_checks():
