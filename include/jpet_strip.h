@@ -100,6 +100,8 @@ typedef struct jpet_strip_counters {
   int64_t n_tiles;           /* non-empty image tiles */
   int64_t n_chunks;          /* work items of the iteration kernel */
   int64_t iterations_done;   /* iterations run since the last set_image */
+  int64_t n_exact_path;      /* events the fast kernel handed to the reference-order
+                                rasteriser (box outside its register-cache shape) */
 } jpet_strip_counters;
 
 /* Version of this ABI (JPET_STRIP_ABI_VERSION). */

@@ -13,6 +13,13 @@
 // held fixed while the kernel sigmas vary.  There is no reference code for this
 // path.
 //
+// The kernel values are evaluated with the accurate exp2f and log1pf (not the
+// .approx hardware forms the MLEM kernel uses): the loss is then a smooth enough
+// function of sigma for central differences of it to match the analytic
+// gradient.  The row prefactor is written as a ratio to the event's own
+// aMa(y), -log2(1 + Q (py^2 - y^2) / aMa(y)) / 2, and the event constant
+// log(c0 / sqrt(aMa(y))) enters the loss in FP64.
+//
 // One warp per event; each row's exact in-ellipse interval is found with the
 // same search as the MLEM row tables (row_interval), so the support is exactly
 // the reference's.  For the events of the tiled chunks the rho window and a
@@ -32,12 +39,7 @@ namespace jpet {
 namespace {
 
 constexpr double kNllLog2e = 1.4426950408889634;
-
-__device__ __forceinline__ float ex2a(float x) {
-  float y;
-  asm("ex2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
+constexpr float kLog2eF = 1.4426950408889634f;
 
 struct NllWindow {
   const float* rho;
@@ -60,7 +62,12 @@ __device__ __forceinline__ void nll_event(const DevGeom& g, const NllConst& k, f
   const float pa_c = 2.0f * sec2 * sec2;     // Pa = pa_c (py^2 + R^2)
   const float qa_c = 4.0f * sec2 * tn * tn;  // Qa = qa_c py^2
   const float ama_ref = pa_c * (y * y + g.radius * g.radius) * k.ipz + qa_c * y * y * k.ipd;
-  const float lref = 0.5f * __log2f(ama_ref);
+  // aMa(py) / aMa(y) = 1 + qq (py - y)(py + y) / aMa(y)
+  const float qq = (pa_c * k.ipz + qa_c * k.ipd) / ama_ref;
+  const double ama_ref_d =
+      (static_cast<double>(pa_c) * (static_cast<double>(y) * y +
+                                    static_cast<double>(g.radius) * g.radius)) * k.ipz +
+      static_cast<double>(qa_c) * y * y * k.ipd;
   const int nrows = box.w - box.y;
   float den = 0.0f, dz = 0.0f, ddl = 0.0f, inv = 0.0f;
   for (int pass = 0; pass < 2; ++pass) {
@@ -80,7 +87,7 @@ __device__ __forceinline__ void nll_event(const DevGeom& g, const NllConst& k, f
       }
       if (lane == 0) {
         // log of the absolute denominator: K = K_ref K', K_ref = c0 / sqrt(aMa(y))
-        loss -= log(dd) + k.log_c0 - 0.5 * log(static_cast<double>(ama_ref));
+        loss -= log(dd) + k.log_c0 - 0.5 * log(ama_ref_d);
         gz -= dzz / dd;
         gdl -= ddd / dd;
       }
@@ -95,14 +102,15 @@ __device__ __forceinline__ void nll_event(const DevGeom& g, const NllConst& k, f
       const float dy = py - y;
       const float pa = pa_c * (py * py + g.radius * g.radius), qa = qa_c * py * py;
       const float ama = pa * k.ipz + qa * k.ipd;
-      const float row_arg = lref - 0.5f * __log2f(ama) + k.kdl * sec2 * dy * dy;
+      const float row_arg =
+          -0.5f * kLog2eF * log1pf(qq * dy * (py + y)) + k.kdl * sec2 * dy * dy;
       const float cz = k.inv_ipz - 0.5f * pa / ama;
       const float cdl = k.half_inv_ipd - 0.5f * qa / ama - 2.0f * sec2 * dy * dy;
       const float u_row = g.tl_z_half_w - z - dy * tn;
       for (int j = lane; j < w; j += 32) {
         const int col = first + j;
         const float u = fmaf(static_cast<float>(col), g.pixel_width, u_row);
-        const float kv = ex2a(fmaf(k.kz * u, u, row_arg));
+        const float kv = exp2f(fmaf(k.kz * u, u, row_arg));
         const int wi = wv.index(iy, col);
         if (pass == 0) {
           const float kr = kv * wv.rho[wi];

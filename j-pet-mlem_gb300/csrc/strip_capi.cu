@@ -24,6 +24,14 @@ namespace {
 
 thread_local std::string g_create_error = "no error";
 
+}  // namespace
+
+namespace jpet {
+void set_call_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace jpet
+
+namespace {
+
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
@@ -108,9 +116,11 @@ struct jpet_strip {
 
 namespace {
 
+}  // namespace
+
 // Scanner<float, short> constructor arithmetic (src/2d/strip/scanner.h:50-67)
 // and GaussianKernel<float> constants (gaussian_kernel.h:27-33), in float.
-DevGeom make_geom(const jpet_strip_geom& in) {
+DevGeom jpet::make_dev_geom(const jpet_strip_geom& in) {
   volatile float R = static_cast<float>(in.radius);
   volatile float L = static_cast<float>(in.scintillator_length);
   volatile float ph = static_cast<float>(in.pixel_height);
@@ -145,6 +155,8 @@ DevGeom make_geom(const jpet_strip_geom& in) {
   g.c0 = static_cast<float>(1 / (2 * M_PI * M_PI) * std::sqrt(static_cast<float>(prod)));
   return g;
 }
+
+namespace {
 
 int validate_geom(const jpet_strip_geom* geom, std::string& msg) {
   if (!geom) {
@@ -437,7 +449,7 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
   h->geom_in = *geom;
   h->opts = o;
   h->device = o.device;
-  h->g = make_geom(*geom);
+  h->g = make_dev_geom(*geom);
   h->fc.kz = -1.4426950408889634f * h->g.ipz;
   h->fc.kdl = -2.0f * 1.4426950408889634f * h->g.ipd;
   h->fc.two_r2 = 2.0f * h->g.radius * h->g.radius;
@@ -650,6 +662,7 @@ int jpet_strip_get_counters(jpet_strip_t* h, jpet_strip_counters* out) {
   out->n_tiles = h->n_tiles_nonempty;
   out->n_chunks = h->n_chunks;
   out->iterations_done = h->iterations_done;
+  out->n_exact_path = static_cast<int64_t>(c.n_exact_path);
   return JPET_OK;
 }
 

@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
   }
   constexpr int kEntRegs = (RS * kRPS + 31) / 32;
   WindowAccess acc{w_rho, w_out, ox, c.oy, pitch};
-  unsigned long long contrib = 0, dummy_calls = 0;
+  unsigned long long contrib = 0, dummy_calls = 0, exact_path = 0;
   int e = warp;
   float4 ev_next = make_float4(0.f, 0.f, 0.f, 0.f);
   short4 box_next = make_short4(0, 0, 0, 0);
@@ -371,6 +371,7 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
     bool ok;
     const uint32_t key = hash32(static_cast<uint32_t>(ei) ^ seed);
     if (nrows > RS * kRPS || maxw + 1 > SW * kCols) {
+      ++exact_path;
       // boxes outside the register-cache shape: reference-order rasteriser;
       // in the fixed-point mode it adds to the global float image directly
       if (ACC == kAccFloat) {
@@ -390,6 +391,7 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
     if (ok && lane == 0) ++contrib;
   }
   if (lane == 0 && contrib) atomicAdd(&counters->n_contributing, contrib);
+  if (lane == 0 && exact_path) atomicAdd(&counters->n_exact_path, exact_path);
   __syncthreads();
   for (int r = warp; r < t.win_h; r += n_warps) {
     const int gy = c.oy + r;

@@ -3,7 +3,11 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
+
 #include <cuda_runtime.h>
+
+#include "../../include/jpet_strip.h"
 
 namespace jpet {
 
@@ -62,9 +66,16 @@ struct DevCounters {
   unsigned long long n_pixels;
   unsigned long long n_kernel_calls;
   unsigned long long n_contributing;
+  unsigned long long n_exact_path;
 };
 
 enum Semantics : int32_t { kCpuReference = 0, kGpuReference = 1 };
+
+// Scanner<float, short> / GaussianKernel<float> constants from the C-ABI geometry
+// (strip_capi.cu).
+DevGeom make_dev_geom(const jpet_strip_geom& in);
+// Message returned by jpet_strip_last_error(NULL) on this thread.
+void set_call_error(const std::string& msg);
 
 constexpr int kHistBins = 4096;  // box width/height histogram bins (last bin: >= 4095)
 

@@ -89,6 +89,7 @@ class Counters(C.Structure):
         ("n_tiles", C.c_int64),
         ("n_chunks", C.c_int64),
         ("iterations_done", C.c_int64),
+        ("n_exact_path", C.c_int64),
     ]
 
 
