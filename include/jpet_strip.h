@@ -188,6 +188,26 @@ int jpet_strip_nll_grad(jpet_strip_t* h, double sigma_z, double sigma_dl, const 
                         const float* d_sens, double* loss, float* d_grad_rho,
                         double* grad_sigma, int64_t* n_skipped);
 
+/* One MLEM iteration that allocates no device memory (no counterpart in the
+ * reference).  For callers that may not allocate device memory, or may not let
+ * a library do so: a process that must not allocate once it is acquiring data,
+ * or an application that owns every device allocation and hands out only input
+ * and output buffers.  d_responses_aos: device AoS (z_u, z_d, dl) float
+ * triples, n <= 1048576 (larger n is rejected with JPET_ERR_ARGUMENT);
+ * d_rho_in / d_rho_out: different device float[n_y*n_z] images; the output is
+ * cleared by the call.  Work runs on cuda_stream (a cudaStream_t, NULL = the
+ * default stream) in the reference's CPU float semantics and operation order;
+ * no handle is involved.  The per-event working data live in one fixed 24 MiB
+ * device array of the library, which every GPU that loads the library keeps
+ * until the process exits; calls share it, so calls that overlap on the GPU
+ * (different streams or unordered host threads) race, while calls ordered on
+ * one stream do not.  The first call on a device looks up the array's address
+ * with that device current; make that first call before any stream capture.
+ * Errors: jpet_strip_last_error(NULL). */
+int jpet_strip_iterate_noalloc(const jpet_strip_geom* geom, const float* d_responses_aos,
+                               int64_t n, const float* d_rho_in, float* d_rho_out,
+                               void* cuda_stream);
+
 /* The full reference GPU entry point over host buffers: uploads the events,
  * starts from rho (in/out, float[n_y*n_z]), runs n_blocks * n_iterations_in_block
  * iterations and calls output(iteration, image, user) at the iterations the

@@ -43,7 +43,7 @@ EXPORTED = [
     "jpet_strip_set_image", "jpet_strip_set_image_device", "jpet_strip_iterate",
     "jpet_strip_get_image", "jpet_strip_image_device", "jpet_strip_get_sensitivity",
     "jpet_strip_get_counters", "jpet_strip_synchronize", "jpet_strip_run",
-    "jpet_strip_nll_grad",
+    "jpet_strip_nll_grad", "jpet_strip_iterate_noalloc",
 ]
 
 
@@ -129,6 +129,7 @@ def lib() -> C.CDLL:
         L.jpet_strip_nll_grad.argtypes = [vp, C.c_double, C.c_double, vp, vp,
                                           C.POINTER(C.c_double), vp, C.POINTER(C.c_double),
                                           C.POINTER(C.c_int64)]
+        L.jpet_strip_iterate_noalloc.argtypes = [C.POINTER(Geom), vp, C.c_int64, vp, vp, vp]
         L.jpet_strip_run.argtypes = [C.POINTER(Geom), C.POINTER(Opts), vp, C.c_int64, vp, C.c_int,
                                      C.c_int, OUTPUT_FN, PROGRESS_FN, vp, C.c_char_p, C.c_size_t]
         for name in EXPORTED:
