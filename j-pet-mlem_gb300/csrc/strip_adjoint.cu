@@ -13,11 +13,14 @@
 // held fixed while the kernel sigmas vary.  There is no reference code for this
 // path.
 //
-// The kernel values are evaluated with the accurate exp2f and log1pf (not the
-// .approx hardware forms the MLEM kernel uses): the loss is then a smooth enough
-// function of sigma for central differences of it to match the analytic
-// gradient.  The row prefactor is written as a ratio to the event's own
-// aMa(y), -log2(1 + Q (py^2 - y^2) / aMa(y)) / 2, and the event constant
+// The loss has to be a smooth function of sigma to the ~1e-9 relative level for
+// central differences with h = 1e-3 mm to resolve it: every sigma-dependent
+// constant is rounded differently at sigma +- h, and a float rounding of, e.g.,
+// ipd shifts log K of every pixel in the same direction.  So the kernel value
+// uses the accurate exp2f (not the .approx form of the MLEM kernel), the row
+// prefactor -log2(aMa(py)/aMa(y))/2 - 2 log2(e) ipd sec^2 dy^2 is computed in
+// FP64 from FP64 constants, the per-pixel coefficient kz = -log2(e) ipz is
+// applied as a float pair (kz + kz_lo), and the event constant
 // log(c0 / sqrt(aMa(y))) enters the loss in FP64.
 //
 // One warp per event; each row's exact in-ellipse interval is found with the
@@ -39,7 +42,6 @@ namespace jpet {
 namespace {
 
 constexpr double kNllLog2e = 1.4426950408889634;
-constexpr float kLog2eF = 1.4426950408889634f;
 
 struct NllWindow {
   const float* rho;
@@ -61,13 +63,13 @@ __device__ __forceinline__ void nll_event(const DevGeom& g, const NllConst& k, f
   const float sec2 = sec * sec;
   const float pa_c = 2.0f * sec2 * sec2;     // Pa = pa_c (py^2 + R^2)
   const float qa_c = 4.0f * sec2 * tn * tn;  // Qa = qa_c py^2
-  const float ama_ref = pa_c * (y * y + g.radius * g.radius) * k.ipz + qa_c * y * y * k.ipd;
-  // aMa(py) / aMa(y) = 1 + qq (py - y)(py + y) / aMa(y)
-  const float qq = (pa_c * k.ipz + qa_c * k.ipd) / ama_ref;
   const double ama_ref_d =
       (static_cast<double>(pa_c) * (static_cast<double>(y) * y +
-                                    static_cast<double>(g.radius) * g.radius)) * k.ipz +
-      static_cast<double>(qa_c) * y * y * k.ipd;
+                                    static_cast<double>(g.radius) * g.radius)) * k.ipz_d +
+      static_cast<double>(qa_c) * y * y * k.ipd_d;
+  // aMa(py) / aMa(y) = 1 + qq (py - y)(py + y)
+  const double qq = (pa_c * k.ipz_d + qa_c * k.ipd_d) / ama_ref_d;
+  const double kdl_sec2 = k.kdl_d * sec2;
   const int nrows = box.w - box.y;
   float den = 0.0f, dz = 0.0f, ddl = 0.0f, inv = 0.0f;
   for (int pass = 0; pass < 2; ++pass) {
@@ -102,15 +104,17 @@ __device__ __forceinline__ void nll_event(const DevGeom& g, const NllConst& k, f
       const float dy = py - y;
       const float pa = pa_c * (py * py + g.radius * g.radius), qa = qa_c * py * py;
       const float ama = pa * k.ipz + qa * k.ipd;
-      const float row_arg =
-          -0.5f * kLog2eF * log1pf(qq * dy * (py + y)) + k.kdl * sec2 * dy * dy;
+      const double dyd = dy;
+      const float row_arg = static_cast<float>(
+          -0.5 * kNllLog2e * log1p(qq * dyd * (static_cast<double>(py) + y)) +
+          kdl_sec2 * dyd * dyd);
       const float cz = k.inv_ipz - 0.5f * pa / ama;
       const float cdl = k.half_inv_ipd - 0.5f * qa / ama - 2.0f * sec2 * dy * dy;
       const float u_row = g.tl_z_half_w - z - dy * tn;
       for (int j = lane; j < w; j += 32) {
         const int col = first + j;
         const float u = fmaf(static_cast<float>(col), g.pixel_width, u_row);
-        const float kv = exp2f(fmaf(k.kz * u, u, row_arg));
+        const float kv = exp2f(fmaf(k.kz * u, u, fmaf(k.kz_lo * u, u, row_arg)));
         const int wi = wv.index(iy, col);
         if (pass == 0) {
           const float kr = kv * wv.rho[wi];
@@ -222,7 +226,10 @@ NllConst make_nll_const(double sigma_z, double sigma_dl) {
   k.ipz = static_cast<float>(ipz);
   k.ipd = static_cast<float>(ipd);
   k.kz = static_cast<float>(-kNllLog2e * ipz);
-  k.kdl = static_cast<float>(-2.0 * kNllLog2e * ipd);
+  k.kz_lo = static_cast<float>(-kNllLog2e * ipz - static_cast<double>(k.kz));
+  k.ipz_d = ipz;
+  k.ipd_d = ipd;
+  k.kdl_d = -2.0 * kNllLog2e * ipd;
   k.inv_ipz = static_cast<float>(1.0 / ipz);
   k.half_inv_ipd = static_cast<float>(0.5 / ipd);
   k.dipz_dsz = static_cast<float>(-2.0 / (sigma_z * sigma_z * sigma_z));

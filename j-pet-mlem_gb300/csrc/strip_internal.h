@@ -114,8 +114,8 @@ cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Til
                                 uint32_t seed, cudaStream_t s);
 // Constants of the likelihood adjoint at the kernel sigmas (strip_adjoint.cu).
 struct NllConst {
-  float ipz, ipd, kz, kdl, inv_ipz, half_inv_ipd, dipz_dsz, dipd_dsdl;
-  double log_c0;
+  float ipz, ipd, kz, kz_lo, inv_ipz, half_inv_ipd, dipz_dsz, dipd_dsdl;
+  double ipz_d, ipd_d, kdl_d, log_c0;
 };
 NllConst make_nll_const(double sigma_z, double sigma_dl);
 // acc[0] -= sum_e log den_e, acc[1..2] -= sum_e (d den_e / d sigma) / den_e,
