@@ -1,9 +1,9 @@
 // Throughput microbenchmarks for the roofline of the strip MLEM kernel.
 //
 // The MLEM iteration is bound by the special-function unit (one exp per
-// kernel-pixel evaluation), FP32 issue and shared-memory atomics, none of which
-// has a measured peak in the pool's peak file.  These kernels measure them on
-// the device the bench runs on:
+// kernel-pixel evaluation), FP32 issue and shared-memory atomics; a copy
+// bandwidth or a GEMM rate says nothing about those units.  These kernels
+// measure them on the device the bench runs on:
 //   ex2     ex2.approx.f32 results per second (MUFU)
 //   ffma    fused multiply-adds per second (FP32 pipe)
 //   atoms   shared-memory float atomicAdd per second (distinct lanes' addresses)

@@ -7,10 +7,16 @@ log-likelihood L(rho, sigma) of the events held by ``rec`` (a
 from the adjoint kernel) and dL/dsigma (FP64).  The 3-sigma support of every
 event is the one of ``rec``'s own sigmas and is held fixed.
 
-``recalibrate_sigma`` alternates MLEM iterations at the current widths (on one
-half of the events) with Newton steps on (sigma_z, sigma_dl) of the likelihood
-of the other half, computed from the adjoint gradient, and re-derives the
-supports at the new widths after every step.
+``calibrate_sigma`` fits (sigma_z, sigma_dl) to the events of a calibration
+source whose activity image is known (a point source at the centre of the field
+of view, say): Newton-preconditioned gradient descent on the likelihood, with the
+gradient from the adjoint kernel.  ``recalibrate_sigma`` is the blind form: it
+alternates MLEM iterations at the current widths (on one half of the events)
+with the same steps on the likelihood of the other half.  The blind form is not
+identifiable: an image blurred by b under widths s predicts the same events as
+the sharp image under widths sqrt(s^2 + b^2), so every width below the true one
+has an image that explains the events equally well, and an MLEM image that is
+still blurred pulls the fit below the true widths.
 """
 from __future__ import annotations
 
@@ -48,17 +54,84 @@ def nll(rec, rho_dev: torch.Tensor, sigma):
     return loss, np.array(gs)
 
 
+def _newton_step(held, rho_dev, sigma, delta, max_step, floor=0.5):
+    """One diagonal Newton step on the widths with backtracking on the loss.
+    Returns (loss at sigma, gradient, accepted step)."""
+    loss, grad = nll(held, rho_dev, sigma)
+    hess = np.zeros(2)
+    for i in range(2):
+        sp, sm = sigma.copy(), sigma.copy()
+        sp[i] += delta
+        sm[i] -= delta
+        hess[i] = (nll(held, rho_dev, sp)[1][i] - nll(held, rho_dev, sm)[1][i]) / (2 * delta)
+    step = np.where(hess > 0, -grad / np.where(hess > 0, hess, 1.0), -np.sign(grad) * max_step)
+    step = np.clip(step, -max_step, max_step)
+    t = 1.0
+    for _ in range(8):
+        trial = sigma + t * step
+        if np.all(trial > floor) and nll(held, rho_dev, trial)[0] <= loss:
+            break
+        t *= 0.5
+    else:
+        t = 0.0
+    return loss, grad, t * step
+
+
+def calibrate_sigma(geom: "capi.Geometry", events: np.ndarray, source_image: np.ndarray, sigma0,
+                    max_steps: int = 20, delta: float = 0.05, max_step: float = 2.0,
+                    tol: float = 1e-3, device: int = 0, log=None):
+    """Estimates (sigma_z, sigma_dl) from the events of a calibration source with
+    a known activity image (float32[n_y, n_z], any scale).
+
+    The likelihood's 3-sigma event supports are those of the widest widths seen
+    so far (sigma0 to start with): they are re-derived only when a width grows
+    past them, so the loss stays one smooth function of sigma between steps.
+    Returns (sigma, history)."""
+    sigma = np.array(sigma0, dtype=np.float64)
+    support = sigma.copy()
+    img = np.ascontiguousarray(source_image, np.float32)
+    if img.shape != (geom.n_y, geom.n_z):
+        raise ValueError("source image must be float32[n_y, n_z]")
+    rho_dev = torch.from_numpy(img * np.float32(len(events) / max(float(img.sum()), 1e-30))).cuda(device)
+    torch.cuda.synchronize(device)
+    history = []
+    held = None
+    try:
+        for k in range(max_steps):
+            if held is None or np.any(sigma > support):
+                support = np.maximum(support, sigma)
+                if held is not None:
+                    held.close()
+                held = capi.StripReconstruction(
+                    capi.Geometry(geom.radius, geom.length, geom.n_y, geom.n_z, geom.pixel,
+                                  float(support[0]), float(support[1])), device=device)
+                held.set_events(events)
+            loss, grad, step = _newton_step(held, rho_dev, sigma, delta, max_step)
+            sigma = sigma + step
+            history.append(dict(iteration=k, loss=loss, sigma=sigma.tolist(), grad=grad.tolist()))
+            if log:
+                log(history[-1])
+            if np.all(np.abs(step) < tol):
+                break
+    finally:
+        if held is not None:
+            held.close()
+    return sigma, history
+
+
 def recalibrate_sigma(geom: "capi.Geometry", events: np.ndarray, sigma0, outer: int = 12,
                       mlem_iterations: int = 5, delta: float = 0.05, max_step: float = 2.0,
                       tol: float = 2e-3, device: int = 0, log=None):
-    """Estimates (sigma_z, sigma_dl) by maximising the list-mode likelihood.
+    """Blind estimate of (sigma_z, sigma_dl) with the image reconstructed at the
+    current widths.
 
     The events are split in two halves.  MLEM reconstructs the image from the
     first half at the current widths; the widths are then fitted to the second,
-    held-out half with the image fixed (diagonal Newton steps from the adjoint
-    gradient, backtracking on the loss).  Fitting the widths to the events the
+    held-out half with the image fixed.  Fitting the widths to the events the
     image was reconstructed from would reward narrower kernels, because MLEM's
-    image sharpens towards those very events.  Returns (sigma, history)."""
+    image sharpens towards those very events.  The result is biased low by the
+    blur left in the MLEM image (see the module docstring).  Returns
+    (sigma, history)."""
     sigma = np.array(sigma0, dtype=np.float64)
     ev_a = np.ascontiguousarray(events[0::2])
     ev_b = np.ascontiguousarray(events[1::2])
@@ -76,27 +149,11 @@ def recalibrate_sigma(geom: "capi.Geometry", events: np.ndarray, sigma0, outer: 
             held.set_events(ev_b)
             rho_dev = torch.from_numpy(rho).cuda(device)
             torch.cuda.synchronize(device)
-            loss, grad = nll(held, rho_dev, sigma)
-            # diagonal Newton step from central differences of the gradient
-            hess = np.zeros(2)
-            for i in range(2):
-                sp, sm = sigma.copy(), sigma.copy()
-                sp[i] += delta
-                sm[i] -= delta
-                hess[i] = (nll(held, rho_dev, sp)[1][i] - nll(held, rho_dev, sm)[1][i]) / (2 * delta)
-            step = np.where(hess > 0, -grad / np.where(hess > 0, hess, 1.0),
-                            -np.sign(grad) * max_step)
-            step = np.clip(step, -max_step, max_step)
-            t = 1.0
-            for _ in range(6):
-                trial = sigma + t * step
-                if np.all(trial > 0.5) and nll(held, rho_dev, trial)[0] <= loss:
-                    break
-                t *= 0.5
-            sigma = sigma + t * step
+            loss, grad, step = _newton_step(held, rho_dev, sigma, delta, max_step)
+            sigma = sigma + step
         history.append(dict(iteration=k, loss=loss, sigma=sigma.tolist(), grad=grad.tolist()))
         if log:
             log(history[-1])
-        if np.all(np.abs(t * step) < tol):
+        if np.all(np.abs(step) < tol):
             break
     return sigma, history

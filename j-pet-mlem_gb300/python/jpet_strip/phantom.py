@@ -209,3 +209,22 @@ def lesion_phantom(seed: int, n_background: int = 10, n_lesions: int = 6,
         base = host[0].intensity if host else big.intensity
         lesions.append(Ellipse(z, y, lesion_radius, lesion_radius, 0.0, contrast * base))
     return lesions + bg
+
+
+def point_source(z: float = -1.0, y: float = -1.0, radius: float = 0.3) -> list[Ellipse]:
+    """Calibration source: one disc of the given radius (mm) at (z, y); the
+    default sits on the centre of the 2 mm pixel next to the middle of the
+    500 x 450 field of view."""
+    return [Ellipse(z, y, radius, radius, 0.0, 1.0)]
+
+
+def point_image(n_y: int, n_z: int, pixel: float, points) -> np.ndarray:
+    """float32[n_y, n_z] image with unit mass in the pixel holding each (z, y);
+    pixel (iy, iz) has its centre at z = (iz + 0.5) p - n_z p / 2,
+    y = n_y p / 2 - (iy + 0.5) p (``src/2d/strip/scanner.h:59-66,136-139``)."""
+    img = np.zeros((n_y, n_z), np.float32)
+    for z, y in points:
+        iz = int(math.floor((z + n_z * pixel / 2) / pixel))
+        iy = int(math.floor((n_y * pixel / 2 - y) / pixel))
+        img[iy, iz] += 1.0
+    return img

