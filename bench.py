@@ -54,7 +54,12 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-peaks", action="store_true", help="skip the peak microbenchmarks")
-    p.add_argument("--variant", type=int, default=0, help="0 fast kernel, 1 exact kernel")
+    p.add_argument("--variant", type=int, default=0,
+                   help="0 fast row-owned kernel, 1 exact kernel, 2 fast warp-per-event kernel")
+    p.add_argument("--block-threads", type=int, default=0,
+                   help="threads per CTA of the iteration kernel (0 = default)")
+    p.add_argument("--raster-shape", type=int, default=0,
+                   help="register shape of the fast kernel (0 auto, 1..6 = 8x1x1 .. 4x2x4)")
     p.add_argument("--precision", type=int, default=0,
                    help="0 FP32 tile sums, 1 compensated tile sums, 2 plus FP64 denominators, "
                         "3 fixed-point tile sums")
@@ -218,7 +223,8 @@ def gb300_arm(args, wl, world, rank, local):
     peaks = None if args.no_peaks else measured_peaks(local)
     stream = torch.cuda.Stream()
     rec = capi.StripReconstruction(geom, device=local, variant=args.variant,
-                                   precision=args.precision)
+                                   precision=args.precision, raster_shape=args.raster_shape,
+                                   block_threads=args.block_threads)
     rec.set_stream(stream.cuda_stream)
     rec.set_events(events)
     with torch.cuda.stream(stream):
@@ -261,7 +267,9 @@ def gb300_arm(args, wl, world, rank, local):
         og = oracle.Geometry(*wl.geometry_args())
         sample = events[:200000]
         with capi.StripReconstruction(geom, device=local, variant=args.variant,
-                                      precision=args.precision) as r2:
+                                      precision=args.precision,
+                                      raster_shape=args.raster_shape,
+                                      block_threads=args.block_threads) as r2:
             r2.set_events(sample)
             r2.iterate(1)
             got = r2.rho.astype(np.float64)
@@ -323,7 +331,8 @@ def gb300_arm(args, wl, world, rank, local):
                     "traffic": None, "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_kind}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "kernel": {"variant": ["fast", "exact"][args.variant],
+        "kernel": {"variant": ["fast", "exact", "warp"][args.variant],
+                   "raster_shape": args.raster_shape, "block_threads": args.block_threads,
                    "precision": ["fp32", "compensated", "fp64_den", "fixed"][args.precision]},
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",

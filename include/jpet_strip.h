@@ -75,8 +75,20 @@ typedef struct jpet_strip_geom {
                                         summed with integer shared atomics; FP64 image */
 
 /* iteration kernel */
-#define JPET_VARIANT_FAST 0  /* exp2-form kernel, packed f32x2, register-cached K*rho (default) */
+#define JPET_VARIANT_FAST 0  /* exp2-form kernel, packed f32x2, register-cached K*rho; image
+                                rows owned by warps, no shared-memory atomics (default) */
 #define JPET_VARIANT_EXACT 1 /* every pixel evaluated in the reference's operation order */
+#define JPET_VARIANT_WARP 2  /* as FAST with one warp per event and shared-memory atomics */
+
+/* register-cache shape of the FAST kernel: G lanes per image row x passes of
+ * 256/G event rows x sweeps of 2G columns (0 = chosen from the event boxes) */
+#define JPET_RASTER_AUTO 0
+#define JPET_RASTER_8x1x1 1 /* <= 32 rows, <= 15 columns */
+#define JPET_RASTER_8x1x2 2 /* <= 32 rows, <= 31 columns */
+#define JPET_RASTER_4x1x2 3 /* <= 64 rows, <= 15 columns */
+#define JPET_RASTER_4x1x3 4 /* <= 64 rows, <= 23 columns */
+#define JPET_RASTER_4x1x4 5 /* <= 64 rows, <= 31 columns */
+#define JPET_RASTER_4x2x4 6 /* <= 128 rows, <= 31 columns */
 
 typedef struct jpet_strip_opts {
   int32_t device;       /* CUDA device ordinal (-D / --cuda-device) */
@@ -86,7 +98,8 @@ typedef struct jpet_strip_opts {
   int32_t tile_h;       /* image tile height in pixels, 0 = chosen by the tuner */
   int32_t block_threads;/* threads per CTA of the iteration kernel, 0 = tuned */
   int32_t variant;      /* JPET_VARIANT_*; the GPU-reference mode always runs EXACT */
-  int32_t reserved[9];  /* must be zero */
+  int32_t raster_shape; /* JPET_RASTER_*; events outside the shape take the exact path */
+  int32_t reserved[8];  /* must be zero */
 } jpet_strip_opts;
 
 /* Per-iteration counters (the reference's ReconstructionStats,
@@ -223,6 +236,104 @@ int jpet_strip_run(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
                    int n_iterations_in_block, jpet_strip_output_fn output,
                    jpet_strip_progress_fn progress, void* user, char* device_name,
                    size_t device_name_len);
+
+/* ---- batched reconstructions ---------------------------------------------
+ * No counterpart in the reference (one event set per process): n independent
+ * reconstructions (own geometry, widths, events, images) whose iterations run
+ * together, one CUDA graph launch per jpet_strip_batch_iterate call.  Every
+ * instance is a handle of its own (jpet_strip_batch_instance) for images,
+ * counters and sensitivity maps; batches run the FP32 row-owned kernel in the
+ * CPU-reference mode. */
+typedef struct jpet_strip_batch jpet_strip_batch_t;
+typedef struct jpet_strip_batch_plan {
+  int32_t raster_shape;          /* JPET_RASTER_* the instance runs (0 = automatic) */
+  int32_t block_threads;         /* CTA size (0 = default) */
+  double tuned_ms_per_iteration; /* best time on the tuning prefix, -1 = not timed */
+  int64_t tuned_events;          /* events of the tuning prefix */
+  int32_t candidates;            /* plans timed for this instance (0 = cached plan) */
+  int32_t reserved;
+} jpet_strip_batch_plan;
+
+/* opts (NULL = defaults) apply to every instance; device = opts->device. */
+int jpet_strip_batch_create(int32_t n, const jpet_strip_geom* geoms, const jpet_strip_opts* opts,
+                            jpet_strip_batch_t** out);
+int jpet_strip_batch_destroy(jpet_strip_batch_t* b);
+const char* jpet_strip_batch_last_error(const jpet_strip_batch_t* b);
+int jpet_strip_batch_size(const jpet_strip_batch_t* b);
+/* The handle of instance i (owned by the batch; do not destroy it). */
+int jpet_strip_batch_instance(jpet_strip_batch_t* b, int32_t i, jpet_strip_t** h);
+/* AoS responses of instance i, host memory (on_device = 0) or device memory. */
+int jpet_strip_batch_set_events(jpet_strip_batch_t* b, int32_t i, const float* aos, int64_t n,
+                                int32_t on_device);
+/* Autotuner: for every instance, times its automatic register shape and the
+ * next larger one with 128- and 256-thread CTAs on the first max_tune_events
+ * events (<= 0: 262144) and keeps the fastest; plans are cached by grid,
+ * pixel size, widths and event-count octave.  Re-bins the events with the
+ * chosen plan and resets every image to uniform 1. */
+int jpet_strip_batch_tune(jpet_strip_batch_t* b, int64_t max_tune_events);
+int jpet_strip_batch_plan_of(const jpet_strip_batch_t* b, int32_t i, jpet_strip_batch_plan* p);
+/* n iterations of every instance: one graph launch (captured on first use for
+ * each n), complete on return. */
+int jpet_strip_batch_iterate(jpet_strip_batch_t* b, int32_t n);
+/* Kernels per batched iteration after the first iterate (0 before). */
+int jpet_strip_batch_launches_per_iteration(const jpet_strip_batch_t* b);
+
+/* ---- event generator (the phantom tool's Monte Carlo on the GPU) ----------
+ * Replaces the emission loop of src/2d/strip/phantom_cmd.cpp:136-444 /
+ * src/common/phantom_monte_carlo.h:33-109 over the regions of
+ * src/2d/geometry/phantom.h:137-181 ("ellipse x y a b angle intensity",
+ * "rectangle x y a b intensity", "point x y intensity"). */
+#define JPET_REGION_ELLIPSE 0   /* centre (x, y) = (z, y), semi-axes a, b, rotation */
+#define JPET_REGION_RECTANGLE 1 /* centre (x, y), half sizes a, b */
+#define JPET_REGION_POINT 2     /* (x, y) */
+typedef struct jpet_strip_region {
+  int32_t kind;      /* JPET_REGION_* */
+  int32_t reserved;  /* must be zero */
+  double x, y, a, b; /* mm */
+  double angle_deg;  /* ellipse rotation in degrees */
+  double intensity;
+} jpet_strip_region;
+
+#define JPET_GEN_DETECTED 1 /* n counts detected events (the reference's --detected);
+                               otherwise n counts emissions over (-pi/2, pi/2) */
+#define JPET_GEN_ADDITIVE 2 /* regions add up instead of earlier ones masking later ones */
+
+/* Count images of the phantom tool (phantom_cmd.cpp:249-352): int32[n_y*n_z]
+ * each (NULL = not wanted) on a grid of geom's n_z x n_y pixels of size
+ * pixel_width whose lower-left corner is -(n_z, n_y) * pixel_width / 2 +
+ * (origin_x, origin_y) (--image-origin); row 0 is the lowest y.  emitted:
+ * emission points of every emission counted; detected: emission points of the
+ * detected events; naive: the points recovered from the smeared responses.
+ * Device pointers for jpet_strip_generate, host pointers for
+ * jpet_strip_generate_host; the device images are accumulated into, the host
+ * ones overwritten. */
+typedef struct jpet_strip_gen_images {
+  int32_t* emitted;
+  int32_t* detected;
+  int32_t* naive;
+  double origin_x, origin_y;
+} jpet_strip_gen_images;
+
+/* Writes the detected, smeared responses (z_u, z_d, dl) as float triples to
+ * the device buffer d_out_aos (room for `capacity` events) in a deterministic
+ * order fixed by (regions, scanner, seed).  geom supplies radius,
+ * scintillator_length, sigma_z and sigma_dl (the pixel fields are unused).
+ * *n_written receives the number of events written: n with
+ * JPET_GEN_DETECTED, else the detected among the first n emissions.  Work
+ * runs on cuda_stream (NULL = the default stream) and is complete on return.
+ * Errors: jpet_strip_last_error(NULL).  No counterpart in the reference's
+ * GPU code (its phantom tool runs on the CPU). */
+int jpet_strip_generate(const jpet_strip_geom* geom, const jpet_strip_region* regions,
+                        int32_t n_regions, int64_t n, uint64_t seed, int32_t flags,
+                        float* d_out_aos, int64_t capacity, int64_t* n_written,
+                        const jpet_strip_gen_images* images, void* cuda_stream);
+/* The same into host memory on device `device` (the library allocates and
+ * frees the device buffers); for callers without a CUDA runtime of their own,
+ * such as the phantom command-line tool. */
+int jpet_strip_generate_host(const jpet_strip_geom* geom, const jpet_strip_region* regions,
+                             int32_t n_regions, int64_t n, uint64_t seed, int32_t flags,
+                             float* out_aos, int64_t capacity, int64_t* n_written,
+                             const jpet_strip_gen_images* images, int32_t device);
 
 #ifdef __cplusplus
 }

@@ -76,6 +76,7 @@ struct jpet_strip {
   DevBuf<int32_t> ev_key, tile_count, tile_offset, tile_cursor, hist, small;
   DevBuf<Chunk> chunks;
   DevBuf<uint16_t> row_table;
+  DevBuf<float2> row_pq;  // per-row exponent coefficients of the row-owned kernel
   FastConst fc{};
   bool use_fast = false;
   bool counters_valid = false;
@@ -186,7 +187,12 @@ int validate_geom(const jpet_strip_geom* geom, std::string& msg) {
 void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
                    const std::vector<int32_t>& hh, int64_t n_nonempty, int n_y, int n_z,
                    Tiling& t) {
-  const int budget_px = 12288;  // per array; two arrays (rho, out) -> 96 KiB per CTA
+  // window pixels per array (rho, out): 12288 (~100 KiB per CTA, 2 CTAs per SM)
+  // for 256-thread CTAs; 6144 (~55 KiB, 4 CTAs per SM) for the row-owned
+  // kernel's 128-thread CTAs
+  const bool rows4 = o.mode == JPET_MODE_CPU_REFERENCE && o.variant == JPET_VARIANT_FAST &&
+                     o.block_threads == 128;
+  const int budget_px = rows4 ? 6144 : 12288;
   auto pct = [&](const std::vector<int32_t>& h, double keep) {
     int64_t tail = static_cast<int64_t>(std::floor((1.0 - keep) * n_nonempty));
     int64_t acc = 0;
@@ -225,17 +231,23 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
   t.chunk_events = 512;
   t.threads = o.block_threads > 0 ? o.block_threads : 256;
   t.group = 32;
-  t.row_stride = (mh + 1) & ~1;
+  // one spare entry per event for its widest row; a multiple of 8 entries so
+  // that every event's table starts on a 16-byte boundary
+  t.row_stride = (mh + 1 + 7) & ~7;
   // register-cache shape of the fast kernel from the rows of 99.9% of the boxes
   // (fast_width_shape adds the widest in-ellipse row)
   const int rows999 = pct(hh, 0.999);
   t.fast_shape = rows999 <= 32 ? kShapeS : (rows999 <= 64 ? kShapeM : kShapeL);
+  t.rows_shape = kRowsShape4x1x3;
 }
 
 // The widest in-ellipse row is 2 * 3 sigma_z / sqrt(2) / pixel (+ rounding).
-int fast_width_shape(const DevGeom& g) {
+int widest_row(const DevGeom& g) {
   const double half = 3.0 * g.sigma_z / std::sqrt(2.0) / g.pixel_width;
-  const int w = 2 * static_cast<int>(half) + 3;
+  return 2 * static_cast<int>(half) + 3;
+}
+int fast_width_shape(const DevGeom& g) {
+  const int w = widest_row(g);
   return w <= 16 ? kShapeS : (w <= 24 ? kShapeM : kShapeL);
 }
 
@@ -275,6 +287,17 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
   for (int b = 1; b < kHistBins; ++b) nonempty += hw[b];
   choose_tiling(h->opts, hw, hh, nonempty, h->g.n_y, h->g.n_z, h->tiling);
   h->tiling.fast_shape = std::max(h->tiling.fast_shape, fast_width_shape(h->g));
+  {
+    int64_t tail = static_cast<int64_t>(std::floor(0.001 * nonempty)), acc_h = 0;
+    int rows999 = 1;
+    for (int b = kHistBins - 1; b > 0; --b) {
+      acc_h += hh[b];
+      if (acc_h > tail) { rows999 = b; break; }
+    }
+    h->tiling.rows_shape = h->opts.raster_shape > 0
+                               ? h->opts.raster_shape - 1
+                               : rows_shape_for(rows999, widest_row(h->g) - 1);
+  }
   const Tiling& t = h->tiling;
   const int32_t n_tiles = t.n_tiles_x * t.n_tiles_y;
   JPET_CUDA(h, h->tile_count.alloc(n_tiles), "cudaMalloc(tiles)");
@@ -328,7 +351,7 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
                                      h->tile_cursor.p, h->sorted_geom.p, h->sorted_box.p,
                                      h->small.p + 1, h->over_geom.p, h->over_box.p, s),
             "scatter_events launch");
-  h->use_fast = h->opts.mode == JPET_MODE_CPU_REFERENCE && h->opts.variant == JPET_VARIANT_FAST;
+  h->use_fast = h->opts.mode == JPET_MODE_CPU_REFERENCE && h->opts.variant != JPET_VARIANT_EXACT;
   h->table_kernel_calls = 0;
   if (h->use_fast && acc > 0) {
     JPET_CUDA(h, h->row_table.alloc(static_cast<size_t>(acc) * t.row_stride),
@@ -337,6 +360,13 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
     JPET_CUDA(h, launch_row_tables(h->g, t, acc, h->sorted_geom.p, h->sorted_box.p,
                                    h->row_table.p, h->box_pixels.p, s),
               "row_table launch");
+    if (h->opts.variant == JPET_VARIANT_FAST) {
+      JPET_CUDA(h, h->row_pq.alloc(static_cast<size_t>(acc) * t.row_stride),
+                "cudaMalloc(row coefficients)");
+      JPET_CUDA(h, launch_row_coefficients(h->g, h->fc, t, acc, h->sorted_geom.p,
+                                           h->sorted_box.p, h->row_table.p, h->row_pq.p, s),
+                "row coefficient launch");
+    }
     JPET_CUDA(h, cudaMemcpyAsync(&h->table_kernel_calls, h->box_pixels.p,
                                  sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
               "copy counter");
@@ -383,6 +413,58 @@ int upload_and_prepare(jpet_strip* h, const float* zu, const float* zd, const fl
 
 }  // namespace
 
+// ---- access for the batch (strip_batch.cu) --------------------------------------
+namespace jpet {
+
+int handle_batch_view(jpet_strip* h, BatchInstance* v, std::string& why) {
+  if (!h->events_ready) {
+    why = "events not set";
+    return JPET_ERR_STATE;
+  }
+  if (!h->use_fast || h->opts.variant != JPET_VARIANT_FAST ||
+      h->opts.precision != JPET_PRECISION_FP32) {
+    why = "batched instances run the FP32 row-owned kernel (CPU-reference mode, FAST variant)";
+    return JPET_ERR_UNSUPPORTED;
+  }
+  v->g = h->g;
+  v->fc = h->fc;
+  v->t = h->tiling;
+  v->chunks = h->chunks.p;
+  v->ev_geom = h->sorted_geom.p;
+  v->ev_box = h->sorted_box.p;
+  v->rows = h->row_table.p;
+  v->pq = h->row_pq.p;
+  v->img[0] = h->rho.p;
+  v->img[1] = h->out.p;
+  v->counters = h->counters.p;
+  v->over_geom = h->over_geom.p;
+  v->over_box = h->over_box.p;
+  v->n_oversize = h->n_oversize;
+  v->n_pix = static_cast<int32_t>(h->g.n_y) * h->g.n_z;
+  return JPET_OK;
+}
+
+int32_t handle_n_chunks(const jpet_strip* h) { return h->n_chunks; }
+int handle_device(const jpet_strip* h) { return h->device; }
+
+// After n batched iterations: the latest image is in img[n & 1].
+void handle_batch_done(jpet_strip* h, int n) {
+  if (n & 1) std::swap(h->rho, h->out);
+  h->iterations_done += n;
+  h->counters_valid = true;
+}
+
+int handle_reprepare(jpet_strip* h, int raster_shape, int block_threads, const float* d_zu,
+                     const float* d_zd, const float* d_dl, int64_t n) {
+  h->opts.raster_shape = raster_shape;
+  h->opts.block_threads = block_threads;
+  return prepare_events(h, d_zu, d_zd, d_dl, n);
+}
+
+const char* handle_error(const jpet_strip* h) { return h->last_error.c_str(); }
+
+}  // namespace jpet
+
 extern "C" {
 
 int jpet_strip_abi_version(void) { return JPET_STRIP_ABI_VERSION; }
@@ -412,8 +494,18 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
     g_create_error = "unknown mode";
     return JPET_ERR_ARGUMENT;
   }
-  if (o.variant != JPET_VARIANT_FAST && o.variant != JPET_VARIANT_EXACT) {
+  if (o.variant != JPET_VARIANT_FAST && o.variant != JPET_VARIANT_EXACT &&
+      o.variant != JPET_VARIANT_WARP) {
     g_create_error = "unknown kernel variant";
+    return JPET_ERR_ARGUMENT;
+  }
+  if (o.mode == JPET_MODE_CPU_REFERENCE && o.variant == JPET_VARIANT_FAST &&
+      o.block_threads != 0 && o.block_threads != 128 && o.block_threads != 256) {
+    g_create_error = "the row-owned kernel runs 128- or 256-thread CTAs";
+    return JPET_ERR_ARGUMENT;
+  }
+  if (o.raster_shape < JPET_RASTER_AUTO || o.raster_shape > JPET_RASTER_4x2x4) {
+    g_create_error = "unknown rasterisation shape";
     return JPET_ERR_ARGUMENT;
   }
   if (o.precision != JPET_PRECISION_FP32 && o.precision != JPET_PRECISION_COMPENSATED &&
@@ -422,7 +514,7 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
     return JPET_ERR_ARGUMENT;
   }
   if (o.precision != JPET_PRECISION_FP32 &&
-      (o.mode != JPET_MODE_CPU_REFERENCE || o.variant != JPET_VARIANT_FAST)) {
+      (o.mode != JPET_MODE_CPU_REFERENCE || o.variant == JPET_VARIANT_EXACT)) {
     g_create_error = "compensated precision modes need the fast kernel and the CPU-reference mode";
     return JPET_ERR_UNSUPPORTED;
   }
@@ -507,6 +599,7 @@ int jpet_strip_destroy(jpet_strip_t* h) {
   h->small.release();
   h->chunks.release();
   h->row_table.release();
+  h->row_pq.release();
   h->box_pixels.release();
   h->nll_acc.release();
   h->nll_grad_tmp.release();
@@ -592,11 +685,19 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
                        : h->opts.precision == JPET_PRECISION_FIXED    ? kPrecisionFixed
                                                                       : kPrecisionFloat;
       const uint32_t seed = 0x9E3779B9u * static_cast<uint32_t>(h->iterations_done + 1);
-      JPET_CUDA(h, launch_iterate_fast(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
-                                       h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
-                                       h->rho.p, h->out.p, h->out64.p, h->counters.p, prec, seed,
-                                       s),
-                "iteration kernel launch");
+      if (h->opts.variant == JPET_VARIANT_WARP) {
+        JPET_CUDA(h, launch_iterate_fast(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
+                                         h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
+                                         h->rho.p, h->out.p, h->out64.p, h->counters.p, prec,
+                                         seed, s),
+                  "iteration kernel launch");
+      } else {
+        JPET_CUDA(h, launch_iterate_rows(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
+                                         h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
+                                         h->row_pq.p, h->rho.p, h->out.p, h->out64.p,
+                                         h->counters.p, prec, seed, s),
+                  "iteration kernel launch");
+      }
     } else {
       JPET_CUDA(h, launch_iterate(h->g, h->tiling, h->opts.mode, h->chunks.p, h->n_chunks,
                                   h->sorted_geom.p, h->sorted_box.p, h->rho.p, sens, h->out.p,

@@ -10,11 +10,13 @@
 //    columns are one interval; it is found from the analytic endpoints
 //    tan*dy +- sqrt((9 - 4 ipd sec^2 dy^2) / (2 ipz)) and corrected by evaluating
 //    the exact test around them.  Stored as 16 bits per row: first column
-//    relative to the box (8 bits) and width (8 bits).  The pixel set of every
+//    relative to the box (8 bits) and width (8 bits); the last entry of the
+//    event's table holds its widest row.  The pixel set of every
 //    event is therefore exactly the reference's, without any per-pixel test in
 //    the iterations.
 //
-// 2. iterate_fast_kernel (every iteration): one CTA per chunk of events of one
+// 2. iterate_fast_kernel (every iteration, the JPET_VARIANT_WARP variant; the
+//    default variant is the row-owned kernel of strip_rows.cu): one CTA per chunk of events of one
 //    image tile, rho window and back-projection window in shared memory (as the
 //    exact kernel).  One warp per event; 4 lanes per image row, 8 rows per step,
 //    each lane two adjacent pixels per 8-column sweep, so that the packed f32x2
@@ -40,22 +42,11 @@
 
 #include "strip_device.cuh"
 #include "strip_internal.h"
+#include "strip_fast_common.cuh"
 #include "strip_raster.cuh"
 
 namespace jpet {
 namespace {
-
-__device__ __forceinline__ float ex2_approx(float x) {
-  float y;
-  asm("ex2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
-__device__ __forceinline__ float lg2_approx(float x) {
-  float y;
-  asm("lg2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
 
 // ---------------------------------------------------------------------------------
 // exact per-row intervals
@@ -78,13 +69,18 @@ __global__ void __launch_bounds__(256) row_table_kernel(DevGeom g, int32_t n, in
     ellipse_abc(g, t, sec, A, B, C);
     const int nrows = b.w - b.y;
     const int bx = b.x, bz = b.z;
+    int maxw = 0;
     for (int ri = lane; ri < nrows; ri += 32) {
       int first;
       const int w = row_interval(g, A, B, C, z, y, t, sec, bx, bz, b.y + ri, first);
       rows[static_cast<size_t>(e) * stride + ri] =
           static_cast<uint16_t>((first - bx) | (w << 8));
       calls += static_cast<unsigned long long>(w);
+      maxw = max(maxw, w);
     }
+    // the last entry of every event holds its widest row (stride > max rows)
+    maxw = __reduce_max_sync(kFull, maxw);
+    if (lane == 0) rows[static_cast<size_t>(e) * stride + stride - 1] = static_cast<uint16_t>(maxw);
   }
   calls = warp_sum_u64(calls);
   if (lane == 0 && calls) atomicAdd(kernel_calls, calls);
@@ -93,54 +89,6 @@ __global__ void __launch_bounds__(256) row_table_kernel(DevGeom g, int32_t n, in
 // ---------------------------------------------------------------------------------
 // fast iteration
 // ---------------------------------------------------------------------------------
-
-constexpr int kG = 4;          // lanes per image row
-constexpr int kRPS = 32 / kG;  // rows per step
-constexpr int kCols = 2 * kG;  // columns per sweep
-
-// Shared-memory window of the fast kernel: origin rounded down to an even
-// column and an even pitch, so that every pixel pair (2k, 2k+1) of a row is one
-// 8-byte aligned ld.shared.v2; 64 floats of padding after the rho window keep
-// the unconditional loads of the last row inside the allocation.  The pitch is
-// 8 mod 16 words: the four rows served by one half-warp (4 lanes x 8 bytes
-// each) then start in four different groups of 8 banks.
-__host__ __device__ inline int fast_pitch(const Tiling& t) {
-  int p = (t.win_w + 2 + 7) & ~7;
-  return (p % 16 == 8) ? p : p + 8;
-}
-__host__ __device__ inline int fast_window_floats(const Tiling& t) {
-  return t.win_h * fast_pitch(t) + 64;
-}
-
-struct FastLane {
-  float2 jf[4], cj[4];  // per-lane pixel offsets j, j+1 and kz pw^2 j^2 per sweep
-};
-
-// Accumulation of the back-projection window.
-//   kAccFloat: float shared-memory atomics (red.shared.add.f32)
-//   kAccCompensated: float shared atomics that return the old value; the exact
-//              rounding error of every addition (Knuth's TwoSum) is added to a
-//              second, compensation window, so sum + compensation carries the
-//              tile total to second order (the compensated-summation idea of
-//              Kahan and Neumaier, made atomic); tiles go to an FP64 image.
-//   kAccFixed: each contribution (a fraction of one event, in [0, 1]) rounded to
-//              22 fractional bits with an unbiased per-event dither and added
-//              with integer shared atomics; a window pixel of a chunk of <= 512
-//              events then stays below 2^31, and its sum is independent of the
-//              order of the additions (deterministic tiles).
-enum Acc : int { kAccFloat = 0, kAccCompensated = 1, kAccFixed = 2 };
-constexpr float kFixedScale = 4194304.0f;     // 2^22
-constexpr float kMagic = 12582912.0f;         // 1.5 * 2^23: float -> integer rounding
-
-__device__ __forceinline__ uint32_t hash32(uint32_t x) {
-  // integer finaliser of MurmurHash3 (public domain, Austin Appleby)
-  x ^= x >> 16;
-  x *= 0x85ebca6bu;
-  x ^= x >> 13;
-  x *= 0xc2b2ae35u;
-  x ^= x >> 16;
-  return x;
-}
 
 // One event on one warp, straight-line code for RS row steps x SW sweeps:
 // phase A computes the constants of 32 rows per pass (one row per lane), phase
@@ -471,6 +419,60 @@ cudaError_t launch_row_tables(const DevGeom& g, const Tiling& t, int32_t n_event
   if (blocks > 152 * 16) blocks = 152 * 16;
   row_table_kernel<<<blocks, 256, 0, s>>>(g, n_events, t.row_stride, ev_geom, ev_box, rows,
                                           kernel_calls);
+  return cudaGetLastError();
+}
+
+// Iteration-invariant exponent coefficients of every (event, row) for the
+// row-owned kernel: with the window origin ox of the event's tile (rounded down
+// to an even column, as the kernel's window) and a = the row's first column
+// rounded down to even, the exponent of the j-th pixel from a is
+// p + q j + kz pw^2 j^2 (the form of fast_event's phase A).
+__global__ void __launch_bounds__(256) row_coeff_kernel(DevGeom g, FastConst fc, Tiling t,
+                                                        int32_t n, int32_t stride,
+                                                        const float4* __restrict__ ev_geom,
+                                                        const short4* __restrict__ ev_box,
+                                                        const uint16_t* __restrict__ rows,
+                                                        float2* __restrict__ pq) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_warps = (gridDim.x * blockDim.x) >> 5;
+  const float kz2pw = 2.0f * fc.kz * g.pixel_width;
+  for (int e = warp; e < n; e += n_warps) {
+    const float4 ev = ev_geom[e];
+    const short4 box = ev_box[e];
+    const float z = ev.x, y = ev.y, tn = ev.z, sec = ev.w;
+    const float sec2 = sec * sec;
+    const float ky = fc.kdl * sec2;
+    const float P = fc.two_r2 * sec2 * sec2 * g.ipz;
+    const float Q = 2.0f * sec2 * sec2 * g.ipz + 4.0f * sec2 * tn * tn * g.ipd;
+    const float lref = 0.5f * lg2_approx(fmaf(Q, y * y, P));
+    const float u_base = g.tl_z_half_w - z;
+    const int ox = ((box.x / t.tile_w) * t.tile_w) & ~1;
+    const int col0 = box.x - ox;
+    const int nrows = box.w - box.y;
+    for (int ri = lane; ri < nrows; ri += 32) {
+      const uint32_t en = rows[static_cast<size_t>(e) * stride + ri];
+      const int lo = col0 + static_cast<int>(en & 255u);
+      const int a_off = lo & ~1;
+      const float py = g.tl_y_half_h - static_cast<float>(box.y + ri) * g.pixel_height;
+      const float dy = py - y;
+      const float lf = lref - 0.5f * lg2_approx(fmaf(Q, py * py, P));
+      const float ua = fmaf(static_cast<float>(ox + a_off), g.pixel_width, u_base - dy * tn);
+      pq[static_cast<size_t>(e) * stride + ri] =
+          make_float2(fmaf(fc.kz * ua, ua, fmaf(ky * dy, dy, lf)), kz2pw * ua);
+    }
+  }
+}
+
+cudaError_t launch_row_coefficients(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                                    int32_t n_events, const float4* ev_geom,
+                                    const short4* ev_box, const uint16_t* rows, float2* pq,
+                                    cudaStream_t s) {
+  if (n_events <= 0) return cudaSuccess;
+  int blocks = (n_events + 7) / 8;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  row_coeff_kernel<<<blocks, 256, 0, s>>>(g, fc, t, n_events, t.row_stride, ev_geom, ev_box,
+                                          rows, pq);
   return cudaGetLastError();
 }
 

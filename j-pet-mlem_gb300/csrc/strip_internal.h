@@ -40,7 +40,8 @@ struct Tiling {
   int32_t threads;         // threads per CTA
   int32_t group;           // lanes per image row in the warp rasteriser (8/16/32)
   int32_t row_stride;      // entries per event in the row table (>= max_box_h, even)
-  int32_t fast_shape;      // register-cache shape of the fast kernel (FastShape)
+  int32_t fast_shape;      // register-cache shape of the warp-per-event kernel (FastShape)
+  int32_t rows_shape;      // register-cache shape of the row-owned kernel (RowsShape)
 };
 
 // Register-cache shapes of the fast iteration kernel: 4 lanes per image row,
@@ -49,6 +50,18 @@ enum FastShape : int32_t {
   kShapeS = 0,  // <= 32 rows, <= 16 columns per row
   kShapeM = 1,  // <= 64 rows, <= 24 columns per row
   kShapeL = 2,  // <= 96 rows, <= 32 columns per row
+};
+
+// Register-cache shapes of the row-owned iteration kernel, named G x RS x SW:
+// G lanes per image row (32 / G rows per warp step, 8 warps, so 256 / G event
+// rows per pass), RS passes, SW sweeps of 2 G columns.
+enum RowsShape : int32_t {
+  kRowsShape8x1x1 = 0,  // <= 32 rows, <= 15 columns per row
+  kRowsShape8x1x2 = 1,  // <= 32 rows, <= 31 columns
+  kRowsShape4x1x2 = 2,  // <= 64 rows, <= 15 columns
+  kRowsShape4x1x3 = 3,  // <= 64 rows, <= 23 columns
+  kRowsShape4x1x4 = 4,  // <= 64 rows, <= 31 columns
+  kRowsShape4x2x4 = 5,  // <= 128 rows, <= 31 columns
 };
 
 // Constants of the fast evaluation: the Gaussian kernel written as
@@ -107,6 +120,17 @@ enum FastPrecision : int32_t {
   kPrecisionCompensatedDen64 = 2,
   kPrecisionFixed = 3,
 };
+cudaError_t launch_row_coefficients(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                                    int32_t n_events, const float4* ev_geom,
+                                    const short4* ev_box, const uint16_t* rows, float2* pq,
+                                    cudaStream_t s);
+int rows_shape_for(int rows999, int width);
+cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                                const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
+                                const short4* ev_box, const uint16_t* rows, const float2* pq,
+                                const float* rho, float* out, double* out64,
+                                DevCounters* counters, int precision, uint32_t seed,
+                                cudaStream_t s);
 cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint16_t* rows, const float* rho,
@@ -140,5 +164,39 @@ cudaError_t launch_iterate_global(const DevGeom& g, int32_t semantics, int32_t n
                                   const float* rho, const float* sens, float* out,
                                   DevCounters* counters, cudaStream_t s);
 cudaError_t launch_sensitivity(const DevGeom& g, int kind, float* out, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Batched reconstructions (strip_batch.cu): what one handle contributes.
+// ---------------------------------------------------------------------------
+struct BatchInstance {
+  DevGeom g;
+  FastConst fc;
+  Tiling t;
+  const Chunk* chunks;
+  const float4* ev_geom;
+  const short4* ev_box;
+  const uint16_t* rows;
+  const float2* pq;
+  float* img[2];  // iteration k reads img[k & 1] and writes img[(k + 1) & 1]
+  DevCounters* counters;
+  const float4* over_geom;
+  const short4* over_box;
+  int32_t n_oversize;
+  int32_t n_pix;
+};
+struct BatchItem {
+  int32_t inst, index;  // chunk (tile kernel) or first large event (large-box kernel)
+};
+constexpr int kBatchOversizePerItem = 32;
+
+cudaError_t batch_rows_prepare(int rows_shape, int threads, size_t smem, int* blocks_per_sm);
+cudaError_t launch_batch_rows(int rows_shape, int threads, size_t smem, int grid,
+                              const BatchInstance* insts, const BatchItem* items, int32_t n_items,
+                              int32_t* next, int parity, cudaStream_t s);
+size_t rows_smem_bytes(const Tiling& t, int threads, int rows_shape);
+cudaError_t launch_batch_clear(const BatchInstance* insts, int32_t n_inst, int32_t max_pix,
+                               int parity, cudaStream_t s);
+cudaError_t launch_batch_oversize(const BatchInstance* insts, const BatchItem* items,
+                                  int32_t n_items, int parity, cudaStream_t s);
 
 }  // namespace jpet

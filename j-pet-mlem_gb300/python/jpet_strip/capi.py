@@ -34,6 +34,9 @@ PRECISION_FP64_DEN = 2
 PRECISION_FIXED = 3
 VARIANT_FAST = 0
 VARIANT_EXACT = 1
+VARIANT_WARP = 2
+RASTER_AUTO = 0
+RASTER_SHAPES = {"8x1x1": 1, "8x1x2": 2, "4x1x2": 3, "4x1x3": 4, "4x1x4": 5, "4x2x4": 6}
 
 # every symbol include/jpet_strip.h declares
 EXPORTED = [
@@ -43,7 +46,11 @@ EXPORTED = [
     "jpet_strip_set_image", "jpet_strip_set_image_device", "jpet_strip_iterate",
     "jpet_strip_get_image", "jpet_strip_image_device", "jpet_strip_get_sensitivity",
     "jpet_strip_get_counters", "jpet_strip_synchronize", "jpet_strip_run",
-    "jpet_strip_nll_grad", "jpet_strip_iterate_noalloc",
+    "jpet_strip_nll_grad", "jpet_strip_iterate_noalloc", "jpet_strip_generate",
+    "jpet_strip_generate_host", "jpet_strip_batch_create", "jpet_strip_batch_destroy",
+    "jpet_strip_batch_last_error", "jpet_strip_batch_size", "jpet_strip_batch_instance",
+    "jpet_strip_batch_set_events", "jpet_strip_batch_tune", "jpet_strip_batch_plan_of",
+    "jpet_strip_batch_iterate", "jpet_strip_batch_launches_per_iteration",
 ]
 
 
@@ -75,7 +82,36 @@ class Opts(C.Structure):
         ("tile_h", C.c_int32),
         ("block_threads", C.c_int32),
         ("variant", C.c_int32),
-        ("reserved", C.c_int32 * 9),
+        ("raster_shape", C.c_int32),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+
+class Region(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("reserved", C.c_int32),
+        ("x", C.c_double),
+        ("y", C.c_double),
+        ("a", C.c_double),
+        ("b", C.c_double),
+        ("angle_deg", C.c_double),
+        ("intensity", C.c_double),
+    ]
+
+
+REGION_ELLIPSE, REGION_RECTANGLE, REGION_POINT = 0, 1, 2
+GEN_DETECTED, GEN_ADDITIVE = 1, 2
+
+
+class BatchPlan(C.Structure):
+    _fields_ = [
+        ("raster_shape", C.c_int32),
+        ("block_threads", C.c_int32),
+        ("tuned_ms_per_iteration", C.c_double),
+        ("tuned_events", C.c_int64),
+        ("candidates", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -130,11 +166,29 @@ def lib() -> C.CDLL:
                                           C.POINTER(C.c_double), vp, C.POINTER(C.c_double),
                                           C.POINTER(C.c_int64)]
         L.jpet_strip_iterate_noalloc.argtypes = [C.POINTER(Geom), vp, C.c_int64, vp, vp, vp]
+        L.jpet_strip_generate.argtypes = [C.POINTER(Geom), C.POINTER(Region), C.c_int32,
+                                          C.c_int64, C.c_uint64, C.c_int32, vp, C.c_int64,
+                                          C.POINTER(C.c_int64), vp, vp]
+        L.jpet_strip_generate_host.argtypes = [C.POINTER(Geom), C.POINTER(Region), C.c_int32,
+                                               C.c_int64, C.c_uint64, C.c_int32, vp, C.c_int64,
+                                               C.POINTER(C.c_int64), vp, C.c_int32]
+        L.jpet_strip_batch_create.argtypes = [C.c_int32, C.POINTER(Geom), C.POINTER(Opts),
+                                              C.POINTER(vp)]
+        L.jpet_strip_batch_destroy.argtypes = [vp]
+        L.jpet_strip_batch_last_error.argtypes = [vp]
+        L.jpet_strip_batch_last_error.restype = C.c_char_p
+        L.jpet_strip_batch_size.argtypes = [vp]
+        L.jpet_strip_batch_instance.argtypes = [vp, C.c_int32, C.POINTER(vp)]
+        L.jpet_strip_batch_set_events.argtypes = [vp, C.c_int32, vp, C.c_int64, C.c_int32]
+        L.jpet_strip_batch_tune.argtypes = [vp, C.c_int64]
+        L.jpet_strip_batch_plan_of.argtypes = [vp, C.c_int32, C.POINTER(BatchPlan)]
+        L.jpet_strip_batch_iterate.argtypes = [vp, C.c_int32]
+        L.jpet_strip_batch_launches_per_iteration.argtypes = [vp]
         L.jpet_strip_run.argtypes = [C.POINTER(Geom), C.POINTER(Opts), vp, C.c_int64, vp, C.c_int,
                                      C.c_int, OUTPUT_FN, PROGRESS_FN, vp, C.c_char_p, C.c_size_t]
         for name in EXPORTED:
             if name not in ("jpet_strip_last_error", "jpet_strip_default_opts",
-                            "jpet_strip_abi_version"):
+                            "jpet_strip_abi_version", "jpet_strip_batch_last_error"):
                 getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -158,12 +212,13 @@ class Geometry:
 
 
 def make_opts(device=0, mode=MODE_CPU_REFERENCE, precision=PRECISION_FP32, tile_w=0,
-              tile_h=0, block_threads=0, variant=VARIANT_FAST) -> Opts:
+              tile_h=0, block_threads=0, variant=VARIANT_FAST, raster_shape=RASTER_AUTO) -> Opts:
     o = Opts()
     lib().jpet_strip_default_opts(C.byref(o))
     o.device, o.mode, o.precision = device, mode, precision
     o.tile_w, o.tile_h, o.block_threads = tile_w, tile_h, block_threads
     o.variant = variant
+    o.raster_shape = raster_shape
     return o
 
 
@@ -175,6 +230,121 @@ def _check(rc: int, h=None):
 
 def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
+
+
+def _regions(regions) -> "C.Array":
+    """Regions as jpet_strip_region: phantom.Ellipse objects or tuples
+    (kind, x, y, a, b, angle_deg, intensity)."""
+    arr = (Region * len(regions))()
+    for i, r in enumerate(regions):
+        if hasattr(r, "angle_deg"):
+            arr[i] = Region(REGION_ELLIPSE, 0, r.z, r.y, r.a, r.b, r.angle_deg, r.intensity)
+        else:
+            kind, x, y, a, b, ang, inten = r
+            arr[i] = Region(int(kind), 0, x, y, a, b, ang, inten)
+    return arr
+
+
+def generate_device(regions, n: int, radius: float, length: float, sigma_z: float,
+                    sigma_dl: float, seed: int, detected: bool = True, additive: bool = False,
+                    device: int = 0):
+    """Events of the phantom regions on the GPU: a torch float32[k, 3] device
+    tensor of (z_u, z_d, dl), k = n with ``detected`` (n detected events), else
+    the detected among n emissions."""
+    import torch
+
+    g = Geom(radius, length, 1, 1, 1.0, 1.0, sigma_z, sigma_dl)
+    regs = _regions(regions)
+    out = torch.empty((max(n, 1), 3), dtype=torch.float32, device=f"cuda:{device}")
+    written = C.c_int64(0)
+    flags = (GEN_DETECTED if detected else 0) | (GEN_ADDITIVE if additive else 0)
+    with torch.cuda.device(device):
+        stream = torch.cuda.current_stream().cuda_stream
+        _check(lib().jpet_strip_generate(C.byref(g), regs, len(regions), n, seed, flags,
+                                         out.data_ptr(), n, C.byref(written), None, stream))
+    return out[: written.value]
+
+
+def generate(regions, n: int, radius: float, length: float, sigma_z: float, sigma_dl: float,
+             seed: int, detected: bool = True, additive: bool = False, device: int = 0) -> np.ndarray:
+    """As generate_device, copied to a host float32[k, 3] array."""
+    return generate_device(regions, n, radius, length, sigma_z, sigma_dl, seed, detected,
+                           additive, device).cpu().numpy()
+
+
+class StripBatch:
+    """Many reconstructions iterated together (one graph launch per iterate)."""
+
+    def __init__(self, geoms, **opts):
+        arr = (Geom * len(geoms))(*[g.c() for g in geoms])
+        o = make_opts(**opts)
+        self._b = C.c_void_p()
+        _check(lib().jpet_strip_batch_create(len(geoms), arr, C.byref(o), C.byref(self._b)), None)
+        self.geoms = list(geoms)
+        self._views = {}
+
+    def _ck(self, rc):
+        if rc != JPET_OK:
+            msg = lib().jpet_strip_batch_last_error(self._b)
+            raise StripError(rc, msg.decode() if msg else "?")
+
+    def close(self):
+        if self._b:
+            lib().jpet_strip_batch_destroy(self._b)
+            self._b = C.c_void_p()
+            self._views = {}
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self.geoms)
+
+    def set_events(self, i: int, events):
+        """events: float32[n, 3] host array, or a CUDA tensor of that shape."""
+        if hasattr(events, "is_cuda") and events.is_cuda:
+            ev = events.contiguous()
+            self._ck(lib().jpet_strip_batch_set_events(self._b, i, ev.data_ptr(), ev.shape[0], 1))
+        else:
+            ev = np.ascontiguousarray(events, dtype=np.float32).reshape(-1, 3)
+            self._ck(lib().jpet_strip_batch_set_events(self._b, i, _ptr(ev) if len(ev) else None,
+                                                       len(ev), 0))
+
+    def tune(self, max_events: int = 0):
+        self._ck(lib().jpet_strip_batch_tune(self._b, max_events))
+
+    def plan(self, i: int) -> dict:
+        p = BatchPlan()
+        self._ck(lib().jpet_strip_batch_plan_of(self._b, i, C.byref(p)))
+        return {f: getattr(p, f) for f, _ in BatchPlan._fields_ if f != "reserved"}
+
+    def iterate(self, n: int = 1):
+        self._ck(lib().jpet_strip_batch_iterate(self._b, n))
+
+    def launches_per_iteration(self) -> int:
+        return lib().jpet_strip_batch_launches_per_iteration(self._b)
+
+    def instance(self, i: int) -> "StripReconstruction":
+        """The instance's handle (owned by the batch)."""
+        if i not in self._views:
+            h = C.c_void_p()
+            self._ck(lib().jpet_strip_batch_instance(self._b, i, C.byref(h)))
+            v = StripReconstruction.__new__(StripReconstruction)
+            v.geom = self.geoms[i]
+            v._h = h
+            v.n_events = 0
+            v._borrowed = True
+            self._views[i] = v
+        return self._views[i]
 
 
 class StripReconstruction:
@@ -189,9 +359,9 @@ class StripReconstruction:
         self.n_events = 0
 
     def close(self):
-        if self._h:
+        if self._h and not getattr(self, "_borrowed", False):
             lib().jpet_strip_destroy(self._h)
-            self._h = C.c_void_p()
+        self._h = C.c_void_p()
 
     def __del__(self):
         try:

@@ -75,3 +75,32 @@ def test_no_device_is_a_status_not_an_abort():
     rc = L.jpet_strip_create(C.byref(g), None, C.byref(h))
     assert rc == capi.JPET_ERR_CUDA
     assert not h.value
+
+
+def test_generator_argument_checks_need_no_device():
+    import ctypes as C
+
+    L = capi.lib()
+    g = capi.Geom(450.0, 1000.0, 1, 1, 1.0, 1.0, 10.0, 42.0)
+    regs = capi._regions([phantom_ellipse()])
+    n = C.c_int64(0)
+    # NULL output with n > 0, zero regions, negative n, bad kind
+    assert L.jpet_strip_generate(C.byref(g), regs, 1, 10, 1, 1, None, 10, C.byref(n), None, None) \
+        == capi.JPET_ERR_ARGUMENT
+    assert L.jpet_strip_generate(C.byref(g), regs, 0, 0, 1, 1, None, 0, C.byref(n), None, None) \
+        == capi.JPET_ERR_ARGUMENT
+    assert L.jpet_strip_generate(C.byref(g), regs, 1, -1, 1, 1, None, 0, C.byref(n), None, None) \
+        == capi.JPET_ERR_ARGUMENT
+    bad = capi._regions([(7, 0.0, 0.0, 1.0, 1.0, 0.0, 1.0)])
+    assert L.jpet_strip_generate(C.byref(g), bad, 1, 0, 1, 1, None, 0, C.byref(n), None, None) \
+        == capi.JPET_ERR_ARGUMENT
+    assert b"region" in L.jpet_strip_last_error(None)
+    # zero events: validated and returns without touching a device
+    assert L.jpet_strip_generate(C.byref(g), regs, 1, 0, 1, 1, None, 0, C.byref(n), None, None) \
+        == capi.JPET_OK
+
+
+def phantom_ellipse():
+    from jpet_strip import phantom
+
+    return phantom.Ellipse(0.0, 0.0, 100.0, 80.0, 10.0, 1.0)

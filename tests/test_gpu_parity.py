@@ -13,7 +13,7 @@ from jpet_strip import capi, phantom
 pytestmark = pytest.mark.gpu
 
 TOL_ITER = 1e-5
-VARIANTS = [capi.VARIANT_FAST, capi.VARIANT_EXACT]
+VARIANTS = [capi.VARIANT_FAST, capi.VARIANT_EXACT, capi.VARIANT_WARP]
 
 
 def rel_l2(a, b):
@@ -246,6 +246,37 @@ def test_fast_kernel_register_shapes(sigma):
     want, st = O.mlem_f(og, ev, 2, threads=8)
     assert rel_l2(got, want) < TOL_ITER
     assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
+
+
+@pytest.mark.parametrize("threads", [128, 256])
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP32, capi.PRECISION_FIXED,
+                                       capi.PRECISION_COMPENSATED, capi.PRECISION_FP64_DEN])
+@pytest.mark.parametrize("shape", sorted(capi.RASTER_SHAPES))
+def test_row_owned_kernel_every_shape(shape, precision, threads):
+    """Every register shape of the default kernel, forced, on 2 mm events whose
+    boxes (64 rows, 22 columns) overflow the small shapes: those events take
+    the queued exact path, the rest the register path; both give the
+    reference's image and counters."""
+    ell = phantom.random_ellipse_phantom(seed=5)
+    ev = phantom.generate_events(ell, 6000, 450.0, 1000.0, 10.0, 42.0, seed=5)
+    args = (450.0, 1000.0, 450, 500, 2.0, 10.0, 42.0)
+    cg, og = capi.Geometry(*args), O.Geometry(*args)
+    want, st = O.mlem_f(og, ev, 1, threads=8)
+    with capi.StripReconstruction(cg, precision=precision, block_threads=threads,
+                                  raster_shape=capi.RASTER_SHAPES[shape]) as rec:
+        rec.set_events(ev)
+        rec.iterate(1)
+        got = rec.rho
+        cnt = rec.counters()
+    # fixed-point tiles round every contribution to 2^-22 of an event: with
+    # 6000 events on 225000 pixels (about 1e-3 of an event per contribution,
+    # ~50 per pixel) that alone is ~1e-5 relative
+    tol = 3e-5 if precision == capi.PRECISION_FIXED else TOL_ITER
+    assert rel_l2(got, want) < tol
+    assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
+    assert cnt["n_contributing"] == st["n_contributing"]
+    small = shape in ("8x1x1", "8x1x2", "4x1x2")
+    assert (cnt["n_exact_path"] > 0) == small, cnt
 
 
 @pytest.mark.parametrize("precision", [capi.PRECISION_COMPENSATED, capi.PRECISION_FP64_DEN,

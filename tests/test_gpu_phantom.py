@@ -1,0 +1,103 @@
+"""GPU event generator (jpet_strip_generate) against the reference's own
+2d_strip_phantom output and the generator's semantics."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from jpet_strip import capi, phantom
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+stats = pytest.importorskip("scipy.stats")
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+R, L = 450.0, 1000.0
+
+
+def _emission_points(ev):
+    """Inverse projection of exact responses (src/2d/strip/response.h:13-37)."""
+    ev = ev.astype(np.float64)
+    t = (ev[:, 0] - ev[:, 1]) / (2 * R)
+    y = -0.5 * ev[:, 2] / np.sqrt(1 + t * t)
+    z = 0.5 * (ev[:, 0] + ev[:, 1] + 2 * y * t)
+    return z, y, t
+
+
+def test_deterministic_for_a_seed():
+    ell = phantom.three_ellipse_phantom()
+    a = capi.generate(ell, 300000, R, L, 10.0, 42.0, seed=5)
+    b = capi.generate(ell, 300000, R, L, 10.0, 42.0, seed=5)
+    c = capi.generate(ell, 300000, R, L, 10.0, 42.0, seed=6)
+    assert a.shape == (300000, 3) and np.isfinite(a).all()
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c)
+    # a shorter request is a prefix of the longer stream
+    d = capi.generate(ell, 1000, R, L, 10.0, 42.0, seed=5)
+    assert np.array_equal(d, a[:1000])
+
+
+def test_distribution_matches_reference_phantom_tool():
+    ref = np.load(os.path.join(GOLDEN, "phantom_ref_events.npy"))
+    ev = capi.generate(phantom.three_ellipse_phantom(), 200000, R, L, 10.0, 42.0, seed=21)
+    for k in range(3):
+        assert stats.ks_2samp(ref[:, k], ev[:, k]).pvalue > 1e-4, k
+    t_ref = (ref[:, 0] - ref[:, 1]) / (2 * R)
+    t_gpu = (ev[:, 0] - ev[:, 1]) / (2 * R)
+    assert stats.ks_2samp(t_ref, t_gpu).pvalue > 1e-4
+
+
+def test_detected_fraction_of_emissions_matches_reference():
+    meta = json.load(open(os.path.join(GOLDEN, "phantom_ref.json")))
+    p_ref = meta["detected"] / meta["emissions"]
+    n = 10_000_000
+    ev = capi.generate_device(phantom.three_ellipse_phantom(), n, R, L, 10.0, 42.0, seed=3,
+                              detected=False)
+    p = ev.shape[0] / n
+    sig = math.sqrt(p_ref * (1 - p_ref) / meta["emissions"] + p * (1 - p) / n)
+    assert abs(p - p_ref) < 5 * sig, (p, p_ref, sig)
+
+
+def test_exact_responses_lie_in_the_regions_with_reference_weights():
+    ell = phantom.three_ellipse_phantom()
+    ev = capi.generate(ell, 200000, R, L, 0.0, 0.0, seed=8)
+    assert (np.abs(ev[:, :2]) < L / 2).all()
+    z, y, _ = _emission_points(ev)
+    member = np.full(len(z), -1)
+    for i in range(len(ell) - 1, -1, -1):
+        inside = ell[i].contains(z, y * (1 - 1e-6))  # float32 responses: tiny slack
+        member[inside] = i
+    assert (member >= 0).mean() > 0.9999
+    # region shares among detected events: same as the CPU generator's
+    ev2 = phantom.generate_events(ell, 200000, R, L, 0.0, 0.0, seed=8)
+    z2, y2, _ = _emission_points(ev2)
+    member2 = np.full(len(z2), -1)
+    for i in range(len(ell) - 1, -1, -1):
+        member2[ell[i].contains(z2, y2)] = i
+    for i in range(len(ell)):
+        p1, p2 = (member == i).mean(), (member2 == i).mean()
+        sig = math.sqrt(p1 * (1 - p1) / len(z) + p2 * (1 - p2) / len(z2))
+        assert abs(p1 - p2) < 5 * sig + 1e-4, (i, p1, p2)
+
+
+def test_point_and_rectangle_regions_and_additive_flag():
+    pts = [(capi.REGION_POINT, 30.0, -20.0, 0, 0, 0, 1.0)]
+    ev = capi.generate(pts, 20000, R, L, 0.0, 0.0, seed=2)
+    z, y, _ = _emission_points(ev)
+    assert np.abs(z - 30.0).max() < 1e-2 and np.abs(y + 20.0).max() < 1e-2
+    rect = [(capi.REGION_RECTANGLE, -50.0, 40.0, 20.0, 10.0, 0, 1.0)]
+    ev = capi.generate(rect, 50000, R, L, 0.0, 0.0, seed=2)
+    z, y, _ = _emission_points(ev)
+    assert (np.abs(z + 50.0) <= 20.0 + 1e-2).all() and (np.abs(y - 40.0) <= 10.0 + 1e-2).all()
+    # an inner disc listed first masks the outer one (disjunctive) unless additive
+    inner = phantom.Ellipse(0.0, 0.0, 50.0, 50.0, 0.0, 1.0)
+    outer = phantom.Ellipse(0.0, 0.0, 100.0, 100.0, 0.0, 1.0)
+    frac = []
+    for additive in (False, True):
+        ev = capi.generate([inner, outer], 200000, R, L, 0.0, 0.0, seed=4, additive=additive)
+        z, y, _ = _emission_points(ev)
+        frac.append((z * z + y * y < 50.0 ** 2).mean())
+    # uniform density: the inner disc holds ~1/4 of the emissions; additive: 2/5
+    assert 0.2 < frac[0] < 0.3 and 0.35 < frac[1] < 0.45, frac

@@ -278,3 +278,23 @@ def test_point_source_likelihood_peaks_at_true_widths():
         vertex = grid[1] + 0.5 * h * (l0 - l2) / (l0 - 2 * l1 + l2)
         assert l0 - 2 * l1 + l2 > 0
         assert abs(vertex - grid[1]) < 0.25, (grid, l0, l1, l2, vertex)
+
+
+def test_cpu_generator_matches_reference_phantom_tool():
+    """The seeded CPU generator that feeds the parity tests draws from the same
+    distribution as the reference's 2d_strip_phantom (two-sample KS against its
+    committed events)."""
+    import os
+
+    from scipy import stats
+
+    from jpet_strip import phantom
+
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "phantom_ref_events.npy"))
+    ev = phantom.generate_events(phantom.three_ellipse_phantom(), 100000, 450.0, 1000.0, 10.0,
+                                 42.0, seed=9)
+    for k in range(3):
+        assert stats.ks_2samp(ref[:, k], ev[:, k]).pvalue > 1e-4, k
+    t_ref = (ref[:, 0] - ref[:, 1]) / 900.0
+    t = (ev[:, 0] - ev[:, 1]) / 900.0
+    assert stats.ks_2samp(t_ref, t).pvalue > 1e-4
