@@ -54,6 +54,13 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-peaks", action="store_true", help="skip the peak microbenchmarks")
+    p.add_argument("--no-batch", action="store_true",
+                   help="skip the batched form (64 reconstructions per graph launch)")
+    p.add_argument("--batch-instances", type=int, default=64)
+    p.add_argument("--sample-events", type=int, default=1_000_000,
+                   help="events of the FP64-oracle prefix in the precision report")
+    p.add_argument("--precision-report", action="store_true",
+                   help="print the precision-stress comparison instead of the headline line")
     p.add_argument("--variant", type=int, default=0,
                    help="0 fast row-owned kernel, 1 exact kernel, 2 fast warp-per-event kernel")
     p.add_argument("--block-threads", type=int, default=0,
@@ -174,14 +181,14 @@ def reference_arm(args, wl, world, rank):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
-    probe_ev = wl.events(min(n_all, 20000))
+    probe_ev = wl.events(min(n_all, 20000), device=None)
     og = oracle.Geometry(*wl.geometry_args())
     t = time.perf_counter()
     oracle.mlem_f(og, probe_ev, 1, threads=threads)
     rate = len(probe_ev) / max(time.perf_counter() - t, 1e-3)
     budget = max(2.0, 120.0 / max(1, args.steps + args.warmup))
     n = int(min(n_all, max(len(probe_ev), rate * budget)))
-    ev = wl.events(n)
+    ev = wl.events(n, device=None)
     rho = None
     for _ in range(args.warmup):
         rho, _ = oracle.mlem_f(og, ev, 1, rho, threads=threads)
@@ -218,7 +225,7 @@ def gb300_arm(args, wl, world, rank, local):
     if world > 1 and not torch.distributed.is_initialized():
         torch.distributed.init_process_group("nccl")
     n_events = args.events or wl.n_events
-    events = wl.events(n_events)
+    events = wl.events(n_events, device=local)
     geom = capi.Geometry(*wl.geometry_args())
     peaks = None if args.no_peaks else measured_peaks(local)
     stream = torch.cuda.Stream()
@@ -311,14 +318,25 @@ def gb300_arm(args, wl, world, rank, local):
 
     if rank != 0:
         return
+    batched = None
+    if not args.no_batch:
+        try:
+            batched = batch_summary(local, k=args.batch_instances)
+        except Exception as exc:  # reported, the headline line still prints
+            batched = {"error": f"{type(exc).__name__}: {exc}"}
     hbm, hbm_kind = hbm_peak()
     roofline = None
     if peaks:
         ex2_peak = peaks["ex2_per_s"]
         atom_peak = peaks["shared_atomic_per_s"]
-        # one exp and one shared-memory atomic per kernel-pixel evaluation: the
-        # lower of the two peaks binds
-        bound_sfu = ex2_peak <= atom_peak
+        if args.variant == 0:
+            # row-owned kernel: one exp per kernel-pixel evaluation and no
+            # shared-memory atomics (plain read-modify-write of owned rows)
+            bound_sfu = True
+        else:
+            # one exp and one shared-memory float atomic per evaluation: the
+            # lower of the two peaks binds
+            bound_sfu = ex2_peak <= atom_peak
         peak = ex2_peak if bound_sfu else atom_peak
         roofline = {"bound": "sfu" if bound_sfu else "shared_atomic",
                     "achieved": evals_per_s / 1e9, "peak": peak / 1e9,
@@ -326,9 +344,10 @@ def gb300_arm(args, wl, world, rank, local):
                     "frac": evals_per_s / peak,
                     "peak_source": "measured on this GPU by libjpet_peaks (ex2.approx and "
                                    "shared float atomicAdd throughput)",
+                    "traffic": profile_traffic(n_events),
                     "sfu_frac": evals_per_s / ex2_peak,
                     "shared_atomic_frac": evals_per_s / atom_peak,
-                    "traffic": None, "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_kind}
+                    "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_kind}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "kernel": {"variant": ["fast", "exact", "warp"][args.variant],
@@ -355,7 +374,163 @@ def gb300_arm(args, wl, world, rank, local):
         "peaks": peaks,
         "counters": counters,
         "kernel_ms_per_iteration": kernel_ms,
+        "batched": batched,
     }
+    print(json.dumps(line), flush=True)
+
+
+def profile_traffic(n_events):
+    """DRAM bytes per iteration-kernel launch from the committed ncu summary of
+    the row-owned kernel (dram__bytes_read.sum + dram__bytes_write.sum of one
+    captured launch), scaled from the captured event count to n_events."""
+    path = os.path.join(ROOT, "profiles", "iterate_rows_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d["dram_bytes_per_launch"] * n_events / d["events"]
+    except (OSError, KeyError, ValueError, ZeroDivisionError):
+        return None
+
+
+def _soa_device(ev):
+    """Device AoS float32[n, 3] -> contiguous SoA rows (z_u, z_d, dl)."""
+    t = ev.t().contiguous()
+    return t, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr()
+
+
+def batch_summary(local, iterations=10, k=64):
+    """Batched form: k reconstructions of uneven sizes, one graph launch per
+    call, untuned and autotuned, against the same instances run one handle
+    at a time (each with its own launches).  Device-resident events; times are
+    host wall-clock around complete calls."""
+    import numpy as np
+    import torch
+
+    from jpet_strip import capi, workloads
+
+    inst = workloads.batch_instances(k)
+    geoms = [capi.Geometry(*wl.geometry_args()) for wl, _ in inst]
+    events = [capi.generate_device(ell, wl.n_events, wl.radius, wl.length, wl.sigma_z,
+                                   wl.sigma_dl, seed=wl.seed, device=local) for wl, ell in inst]
+    n_total = int(sum(e.shape[0] for e in events))
+    ones = [np.ones((g.n_y, g.n_z), np.float32) for g in geoms]
+    # one handle at a time
+    single_s = 0.0
+    single_imgs = []
+    evals = 0
+    for g, ev, one in zip(geoms, events, ones):
+        t, zu, zd, dl = _soa_device(ev)
+        with capi.StripReconstruction(g, device=local) as r:
+            r.set_events_device(zu, zd, dl, ev.shape[0])
+            r.iterate(1)
+            r.rho = one
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r.iterate(iterations)
+            r.synchronize()
+            single_s += time.perf_counter() - t0
+            single_imgs.append(r.rho)
+            evals += r.counters()["n_kernel_calls"]
+        del t
+    out = {"instances": k, "events": n_total, "iterations": iterations,
+           "kernel_pixel_evals_per_iteration": int(evals),
+           "single_handles": {"seconds": single_s,
+                              "value": n_total * iterations / single_s}}
+    with capi.StripBatch(geoms, device=local) as b:
+        for i, ev in enumerate(events):
+            b.set_events(i, ev)
+        for label in ("batched", "batched_tuned"):
+            if label == "batched_tuned":
+                t0 = time.perf_counter()
+                b.tune()
+                out["tune_seconds"] = time.perf_counter() - t0
+            b.iterate(iterations)  # builds the work list and captures the graph
+            for i in range(k):
+                b.instance(i).rho = ones[i]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.iterate(iterations)
+            dt = time.perf_counter() - t0
+            err = max(float(np.linalg.norm(b.instance(i).rho.astype(np.float64) - single_imgs[i])
+                            / max(np.linalg.norm(single_imgs[i]), 1e-30)) for i in range(k))
+            out[label] = {"seconds": dt, "value": n_total * iterations / dt,
+                          "graph_launches": 1,
+                          "kernels_per_iteration": b.launches_per_iteration(),
+                          "max_rel_l2_vs_single_handles": err}
+        plans = {}
+        for i in range(k):
+            p = b.plan(i)
+            key = f"shape{p['raster_shape']}x{p['block_threads']}"
+            plans[key] = plans.get(key, 0) + 1
+        out["tuned_plans"] = plans
+    out["speedup_tuned_vs_single"] = out["single_handles"]["seconds"] / out["batched_tuned"]["seconds"]
+    return out
+
+
+def precision_report(args, local):
+    """Precision stress: the 1 mm lesion workload in every accumulation mode.
+    Full scale: time per iteration and the image differences between modes;
+    a fixed 1e6-event prefix: each mode against the FP64 oracle (the
+    reference's algorithm in double) and the reference float path."""
+    import numpy as np
+    import torch
+
+    from jpet_strip import capi
+    from jpet_strip.workloads import WORKLOADS
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    wl = WORKLOADS["stress-1mm-100M"]
+    n = args.events or wl.n_events
+    iters = wl.iterations
+    geom = capi.Geometry(*wl.geometry_args())
+    modes = [("fp32", capi.PRECISION_FP32), ("compensated", capi.PRECISION_COMPENSATED),
+             ("compensated_fp64_den", capi.PRECISION_FP64_DEN), ("fixed", capi.PRECISION_FIXED)]
+    ev = capi.generate_device(wl.ellipses(), n, wl.radius, wl.length, wl.sigma_z, wl.sigma_dl,
+                              seed=wl.seed, device=local)
+    t, zu, zd, dl = _soa_device(ev)
+    full = {}
+    imgs = {}
+    for name, prec in modes:
+        with capi.StripReconstruction(geom, device=local, precision=prec) as r:
+            r.set_events_device(zu, zd, dl, n)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r.iterate(iters)
+            r.synchronize()
+            dt = time.perf_counter() - t0
+            imgs[name] = r.rho.astype(np.float64)
+            full[name] = {"ms_per_iteration": 1e3 * dt / iters,
+                          "value": n * iters / dt}
+    ref = imgs["compensated_fp64_den"]
+    for name in imgs:
+        d = imgs[name] - ref
+        full[name]["rel_l2_vs_compensated_fp64_den"] = float(np.linalg.norm(d) / np.linalg.norm(ref))
+        full[name]["max_abs_vs_compensated_fp64_den"] = float(np.abs(d).max())
+    del t
+    m = min(n, args.sample_events)
+    sample = ev[:m].cpu().numpy()
+    og = oracle.Geometry(*wl.geometry_args())
+    threads = os.cpu_count() or 1
+    f64 = oracle.mlem_d(og, sample, iters, threads=threads)
+    f32, _ = oracle.mlem_f(og, sample, iters, threads=threads)
+    sub = {"reference_float": {"rel_l2_vs_fp64": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
+                               "max_abs_vs_fp64": float(np.abs(f32 - f64).max())}}
+    for name, prec in modes:
+        with capi.StripReconstruction(geom, device=local, precision=prec) as r:
+            r.set_events(sample)
+            r.iterate(iters)
+            g = r.rho.astype(np.float64)
+        sub[name] = {"rel_l2_vs_fp64": float(np.linalg.norm(g - f64) / np.linalg.norm(f64)),
+                     "max_abs_vs_fp64": float(np.abs(g - f64).max())}
+    line = {"metric": "precision stress: rel L2 / max-abs vs FP64 per accumulation mode",
+            "config": {"workload": wl.name, "events": n, "grid": f"{wl.n_z}x{wl.n_y}",
+                       "pixel_mm": wl.pixel, "sigma_z": wl.sigma_z, "sigma_dl": wl.sigma_dl,
+                       "phantom": "10 random ellipses + 6 lesions of 5 mm at 8x",
+                       "iterations": iters},
+            "full_scale": full,
+            "fp64_oracle_sample": {"events": m, "iterations": iters, "modes": sub}}
     print(json.dumps(line), flush=True)
 
 
@@ -367,6 +542,8 @@ def main():
     world, rank, local = dist_env()
     if args.impl == "reference":
         reference_arm(args, wl, world, rank)
+    elif args.precision_report:
+        precision_report(args, local)
     else:
         gb300_arm(args, wl, world, rank, local)
 

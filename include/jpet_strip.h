@@ -96,7 +96,8 @@ typedef struct jpet_strip_opts {
   int32_t precision;    /* JPET_PRECISION_* */
   int32_t tile_w;       /* image tile width in pixels, 0 = chosen by the tuner */
   int32_t tile_h;       /* image tile height in pixels, 0 = chosen by the tuner */
-  int32_t block_threads;/* threads per CTA of the iteration kernel, 0 = tuned */
+  int32_t block_threads;/* threads per CTA of the iteration kernel, 0 = default (128 for
+                           the FAST kernel, which also takes 256; 256 otherwise) */
   int32_t variant;      /* JPET_VARIANT_*; the GPU-reference mode always runs EXACT */
   int32_t raster_shape; /* JPET_RASTER_*; events outside the shape take the exact path */
   int32_t reserved[8];  /* must be zero */

@@ -191,7 +191,7 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
   // for 256-thread CTAs; 6144 (~55 KiB, 4 CTAs per SM) for the row-owned
   // kernel's 128-thread CTAs
   const bool rows4 = o.mode == JPET_MODE_CPU_REFERENCE && o.variant == JPET_VARIANT_FAST &&
-                     o.block_threads == 128;
+                     o.block_threads != 256;
   const int budget_px = rows4 ? 6144 : 12288;
   auto pct = [&](const std::vector<int32_t>& h, double keep) {
     int64_t tail = static_cast<int64_t>(std::floor((1.0 - keep) * n_nonempty));
@@ -229,7 +229,7 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
   t.n_tiles_x = (n_z + tw - 1) / tw;
   t.n_tiles_y = (n_y + th - 1) / th;
   t.chunk_events = 512;
-  t.threads = o.block_threads > 0 ? o.block_threads : 256;
+  t.threads = o.block_threads > 0 ? o.block_threads : (rows4 ? 128 : 256);
   t.group = 32;
   // one spare entry per event for its widest row; a multiple of 8 entries so
   // that every event's table starts on a 16-byte boundary

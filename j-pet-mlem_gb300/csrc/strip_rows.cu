@@ -486,7 +486,8 @@ cudaError_t launch_rows_prec(const DevGeom& g, const FastConst& fc, const Tiling
   }
 }
 
-// CTAs of 4 warps (the default) or 8 warps (Tiling::threads = 256)
+// CTAs of 4 warps (the default: 4 CTAs of ~55 KiB per SM) or 8 warps
+// (Tiling::threads = 256, 2 CTAs of ~100 KiB per SM)
 template <int G, int ROWS, int SW>
 cudaError_t launch_rows_shape(const DevGeom& g, const FastConst& fc, const Tiling& t,
                               const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,

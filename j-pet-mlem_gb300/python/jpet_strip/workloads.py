@@ -31,13 +31,57 @@ class Workload:
             return phantom.lesion_phantom(self.seed)
         return phantom.random_ellipse_phantom(self.seed)
 
-    def events(self, n: int | None = None):
-        return phantom.generate_events(self.ellipses(), n or self.n_events, self.radius,
-                                       self.length, self.sigma_z, self.sigma_dl, seed=self.seed)
+    def events(self, n: int | None = None, device: int | None = 0):
+        """Detected responses float32[n, 3].  With a CUDA device the GPU generator
+        (capi.generate) draws them; without one, the seeded CPU generator (the
+        same distribution, another random stream)."""
+        n = n or self.n_events
+        if device is not None:
+            try:
+                import torch
+
+                if torch.cuda.is_available():
+                    from . import capi
+
+                    return capi.generate(self.ellipses(), n, self.radius, self.length,
+                                         self.sigma_z, self.sigma_dl, seed=self.seed,
+                                         device=device)
+            except ImportError:
+                pass
+        return phantom.generate_events(self.ellipses(), n, self.radius, self.length,
+                                       self.sigma_z, self.sigma_dl, seed=self.seed)
 
     def geometry_args(self):
         return (self.radius, self.length, self.n_y, self.n_z, self.pixel, self.sigma_z,
                 self.sigma_dl)
+
+
+def batch_instances(k: int = 64, seed0: int = 100, max_events: int = 5_000_000,
+                    min_events: int = 10_000):
+    """The batched workload: k independent reconstructions with seeds seed0..,
+    event counts log-uniform in [min_events, max_events], grids of n_z in
+    100..500 by n_y in 100..450 pixels at 2..5 mm, sigma_z in [6, 14] mm,
+    sigma_dl in [30, 60] mm and 1..10 random ellipses inside the part of the
+    grid the scanner sees.  Returns [(Workload, ellipses)]."""
+    import numpy as np
+
+    out = []
+    for i in range(k):
+        rng = np.random.default_rng(seed0 + i)
+        p = float(rng.integers(2, 6))
+        n_z = int(rng.integers(100, 501))
+        n_y = int(rng.integers(100, 451))
+        sz = float(rng.uniform(6.0, 14.0))
+        sdl = float(rng.uniform(30.0, 60.0))
+        n = int(np.exp(rng.uniform(np.log(min_events), np.log(max_events))))
+        hz, hy = min(n_z * p / 2, 500.0), min(n_y * p / 2, 450.0)
+        ell = phantom.random_ellipse_phantom(seed0 + i, n=int(rng.integers(1, 11)), half_z=hz,
+                                             half_y=hy, centre_z=0.6 * hz, centre_y=0.6 * hy,
+                                             axes=(10.0, 0.8 * min(hz, hy)))
+        wl = Workload(f"batch-{i}", 450.0, 1000.0, n_y, n_z, p, sz, sdl, n, 10, seed0 + i,
+                      "custom")
+        out.append((wl, ell))
+    return out
 
 
 WORKLOADS = {
