@@ -88,3 +88,59 @@ def test_gpu_mode_output_protocol(tmp_path, golden):
     # sensitivity, iterations 1..3 of block 0 (i < I-1 and the block end), block end 6
     assert names == ["g_1.bin", "g_2.bin", "g_3.bin", "g_6.bin", "g_sensitivity.bin"]
     assert "# device:" in r.stderr
+
+
+PHANTOM_TOOL = os.path.join(ROOT, "j-pet-mlem_gb300", "bin", "2d_strip_phantom")
+
+
+def run_phantom(args, cwd=None):
+    return subprocess.run([PHANTOM_TOOL] + args, capture_output=True, text=True, cwd=cwd,
+                          timeout=300)
+
+
+def test_phantom_tool_usage_and_errors(tmp_path):
+    r = run_phantom([])
+    assert r.returncode == 0
+    for opt in ["--n-emissions", "--additive", "--detected", "--point", "--scale", "--output",
+                "--image-origin", "--seed"]:
+        assert opt in r.stderr
+    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "-e", "10"])
+    assert r.returncode == 1 and "at least one input phantom description expected" in r.stderr
+    (tmp_path / "bad.txt").write_text("hexagon 0 0 1 1 1\n")
+    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "-e", "10", str(tmp_path / "bad.txt")])
+    assert r.returncode == 1 and "unknown phantom type: hexagon" in r.stderr
+    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "-e", "10", "--full",
+                     str(tmp_path / "bad.txt")])
+    assert r.returncode == 1 and "not supported" in r.stderr
+
+
+@pytest.mark.gpu
+def test_phantom_then_reconstruction_tool_chain(tmp_path):
+    """2d_strip_phantom writes events, .cfg and count images; the reconstruction
+    tool reads the events and loads the scanner options from the .cfg."""
+    golden = os.path.join(ROOT, "tests", "golden", "phantom_three.txt")
+    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "--n-z-pixels", "200",
+                     "--n-y-pixels", "180", "--s-z", "10", "--s-dl", "42", "-e", "200000",
+                     "--seed", "7", "-o", str(tmp_path / "ph.bin"), golden])
+    assert r.returncode == 0, r.stderr
+    ev = np.fromfile(tmp_path / "ph.bin", np.float32).reshape(-1, 3)
+    det = np.fromfile(tmp_path / "ph_detected", np.int32).reshape(180, 200)
+    emi = np.fromfile(tmp_path / "ph_emitted", np.int32).reshape(180, 200)
+    naive = np.fromfile(tmp_path / "ph_naive", np.int32).reshape(180, 200)
+    assert 0.40 < len(ev) / 200000 < 0.44  # the reference detects ~0.420 of the emissions
+    assert det.sum() == len(ev) and emi.sum() == 200000 and 0.9 * len(ev) < naive.sum() <= len(ev)
+    cfg = (tmp_path / "ph.cfg").read_text()
+    assert "--radius=450" in cfg and "--s-dl=42" in cfg and "--n-emissions=200000" in cfg
+    assert "sizes: 200 180" in (tmp_path / "ph_detected.nrrd").read_text()
+    # same seed, same stream; the text output holds the same events
+    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "--n-z-pixels", "200",
+                     "--n-y-pixels", "180", "--s-z", "10", "--s-dl", "42", "-e", "200000",
+                     "--seed", "7", "-o", str(tmp_path / "ph2.txt"), golden])
+    assert r.returncode == 0, r.stderr
+    ev2 = np.loadtxt(tmp_path / "ph2.txt", dtype=np.float32).reshape(-1, 3)
+    assert ev2.shape == ev.shape and np.allclose(ev2, ev, rtol=1e-5, atol=1e-3)
+    # reconstruction with the options of the accompanying .cfg only
+    r = run([str(tmp_path / "ph.bin"), "-i", "2", "-I", "1", "-o", str(tmp_path / "r.bin")])
+    assert r.returncode == 0, r.stderr
+    img = np.fromfile(tmp_path / "r_2.bin", np.float32).reshape(180, 200)
+    assert abs(img.sum() - len(ev)) < 1e-3 * len(ev)
