@@ -402,7 +402,9 @@ def batch_summary(local, iterations=10, k=64):
     """Batched form: k reconstructions of uneven sizes, one graph launch per
     call, untuned and autotuned, against the same instances run one handle
     at a time (each with its own launches).  Device-resident events; times are
-    host wall-clock around complete calls."""
+    host wall-clock around complete calls.  Images are compared after one
+    iteration (float summation order only) and after `iterations` (where MLEM
+    amplifies those differences, as between two runs of one handle)."""
     import numpy as np
     import torch
 
@@ -417,12 +419,14 @@ def batch_summary(local, iterations=10, k=64):
     # one handle at a time
     single_s = 0.0
     single_imgs = []
+    single_one = []
     evals = 0
     for g, ev, one in zip(geoms, events, ones):
         t, zu, zd, dl = _soa_device(ev)
         with capi.StripReconstruction(g, device=local) as r:
             r.set_events_device(zu, zd, dl, ev.shape[0])
             r.iterate(1)
+            single_one.append(r.rho)
             r.rho = one
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -439,6 +443,10 @@ def batch_summary(local, iterations=10, k=64):
     with capi.StripBatch(geoms, device=local) as b:
         for i, ev in enumerate(events):
             b.set_events(i, ev)
+        b.iterate(1)  # one batched iteration from the uniform image
+        out["max_rel_l2_vs_single_handles_1_iteration"] = max(
+            float(np.linalg.norm(b.instance(i).rho.astype(np.float64) - single_one[i])
+                  / max(np.linalg.norm(single_one[i]), 1e-30)) for i in range(k))
         for label in ("batched", "batched_tuned"):
             if label == "batched_tuned":
                 t0 = time.perf_counter()
@@ -469,9 +477,10 @@ def batch_summary(local, iterations=10, k=64):
 
 def precision_report(args, local):
     """Precision stress: the 1 mm lesion workload in every accumulation mode.
-    Full scale: time per iteration and the image differences between modes;
-    a fixed 1e6-event prefix: each mode against the FP64 oracle (the
-    reference's algorithm in double) and the reference float path."""
+    Full scale: time per iteration and each image against the reference
+    iteration at double on the GPU (jpet_strip_reference_fp64); a fixed
+    1e6-event prefix: each mode, and that GPU FP64 iteration, against the CPU
+    FP64 oracle (the reference's algorithm in double)."""
     import numpy as np
     import torch
 
@@ -503,11 +512,17 @@ def precision_report(args, local):
             imgs[name] = r.rho.astype(np.float64)
             full[name] = {"ms_per_iteration": 1e3 * dt / iters,
                           "value": n * iters / dt}
-    ref = imgs["compensated_fp64_den"]
+    # the FP64 yardstick at full scale: the reference iteration at double on the GPU
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref64, _ = capi.reference_fp64(geom, ev, iters, device=local)
+    fp64_s = time.perf_counter() - t0
     for name in imgs:
-        d = imgs[name] - ref
-        full[name]["rel_l2_vs_compensated_fp64_den"] = float(np.linalg.norm(d) / np.linalg.norm(ref))
-        full[name]["max_abs_vs_compensated_fp64_den"] = float(np.abs(d).max())
+        d = imgs[name] - ref64
+        full[name]["rel_l2_vs_fp64"] = float(np.linalg.norm(d) / np.linalg.norm(ref64))
+        full[name]["max_abs_vs_fp64"] = float(np.abs(d).max())
+    full["fp64_reference"] = {"ms_per_iteration": 1e3 * fp64_s / iters,
+                              "value": n * iters / fp64_s}
     del t
     m = min(n, args.sample_events)
     sample = ev[:m].cpu().numpy()
@@ -524,6 +539,9 @@ def precision_report(args, local):
             g = r.rho.astype(np.float64)
         sub[name] = {"rel_l2_vs_fp64": float(np.linalg.norm(g - f64) / np.linalg.norm(f64)),
                      "max_abs_vs_fp64": float(np.abs(g - f64).max())}
+    g64, _ = capi.reference_fp64(geom, sample, iters, device=local)
+    sub["fp64_reference_gpu"] = {"rel_l2_vs_fp64": float(np.linalg.norm(g64 - f64) / np.linalg.norm(f64)),
+                                 "max_abs_vs_fp64": float(np.abs(g64 - f64).max())}
     line = {"metric": "precision stress: rel L2 / max-abs vs FP64 per accumulation mode",
             "config": {"workload": wl.name, "events": n, "grid": f"{wl.n_z}x{wl.n_y}",
                        "pixel_mm": wl.pixel, "sigma_z": wl.sigma_z, "sigma_dl": wl.sigma_dl,

@@ -238,6 +238,17 @@ int jpet_strip_run(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
                    jpet_strip_progress_fn progress, void* user, char* device_name,
                    size_t device_name_len);
 
+/* The reference iteration at double on the GPU (Reconstruction<double,
+ * GaussianKernel<double>>, reconstruction.h:108-154): the FP64 yardstick for
+ * accuracy studies at full event counts.  n_iterations iterations of the
+ * device AoS responses from d_rho (in/out, double[n_y*n_z]); d_work is a
+ * second double[n_y*n_z] buffer.  Counters of the last iteration are optional.
+ * Runs on cuda_stream and is complete on return.  No counterpart in the
+ * reference's GPU code. */
+int jpet_strip_reference_fp64(const jpet_strip_geom* geom, const float* d_responses_aos,
+                              int64_t n, double* d_rho, double* d_work, int32_t n_iterations,
+                              int64_t* kernel_calls, int64_t* contributing, void* cuda_stream);
+
 /* ---- batched reconstructions ---------------------------------------------
  * No counterpart in the reference (one event set per process): n independent
  * reconstructions (own geometry, widths, events, images) whose iterations run

@@ -4,7 +4,7 @@
 // kernel-pixel evaluation), FP32 issue and shared-memory atomics; a copy
 // bandwidth or a GEMM rate says nothing about those units.  These kernels
 // measure them on the device the bench runs on:
-//   ex2     ex2.approx.f32 results per second (MUFU)
+//   ex2     ex2.approx.ftz.f32 results per second (MUFU; the form the kernels use)
 //   ffma    fused multiply-adds per second (FP32 pipe)
 //   atoms   shared-memory float atomicAdd per second (distinct lanes' addresses)
 //   red     global float atomicAdd per second to an L2-resident buffer
@@ -18,7 +18,7 @@ namespace {
 
 __device__ __forceinline__ float ex2_approx(float x) {
   float y;
-  asm volatile("ex2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 

@@ -9,15 +9,19 @@
 
 namespace jpet {
 
+// 2^x and log2(x) on the special-function unit, subnormal inputs and results
+// flushed to zero (.ftz): the fast kernels evaluate them on normal values only
+// (kernel ratios >= ~1e-2 and positive aMa terms), and without .ftz every call
+// also pays for a range test and two rescaling multiplies.
 __device__ __forceinline__ float ex2_approx(float x) {
   float y;
-  asm("ex2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 
 __device__ __forceinline__ float lg2_approx(float x) {
   float y;
-  asm("lg2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 

@@ -269,7 +269,7 @@ __device__ __forceinline__ void rows_chunk(
         const int w = rv ? static_cast<int>(en >> 8) : 0;
         const int lo = col0 + static_cast<int>(en & 255u);
         const int a_off = lo & ~1;
-        const int lead = lo - a_off;  // 0 or 1 pixels before the interval
+        const int lead = lo & 1;  // 0 or 1 pixels before the interval
         const int end = lead + w;
         const int bse = (r0 + ric) * pitch + a_off + 2 * gl;
         base[j][rs] = bse;
@@ -280,7 +280,8 @@ __device__ __forceinline__ void rows_chunk(
           const float2 a = __ffma2_rn(q2, jf[s], __fadd2_rn(p2, cj[s]));
           const float2 r2 = *reinterpret_cast<const float2*>(w_rho + bse + kSweep * s);
           float2 kr = __fmul2_rn(make_float2(ex2_approx(a.x), ex2_approx(a.y)), r2);
-          kr.x = (k0 >= lead && k0 < end) ? kr.x : 0.0f;
+          // only the first pixel of the row can lie before the interval
+          kr.x = ((s > 0 || k0 >= lead) && k0 < end) ? kr.x : 0.0f;
           kr.y = (k0 + 1 < end) ? kr.y : 0.0f;
           cache[j][rs][s] = kr;
           den_a = __fadd2_rn(den_a, kr);

@@ -51,6 +51,7 @@ EXPORTED = [
     "jpet_strip_batch_last_error", "jpet_strip_batch_size", "jpet_strip_batch_instance",
     "jpet_strip_batch_set_events", "jpet_strip_batch_tune", "jpet_strip_batch_plan_of",
     "jpet_strip_batch_iterate", "jpet_strip_batch_launches_per_iteration",
+    "jpet_strip_reference_fp64",
 ]
 
 
@@ -184,6 +185,8 @@ def lib() -> C.CDLL:
         L.jpet_strip_batch_plan_of.argtypes = [vp, C.c_int32, C.POINTER(BatchPlan)]
         L.jpet_strip_batch_iterate.argtypes = [vp, C.c_int32]
         L.jpet_strip_batch_launches_per_iteration.argtypes = [vp]
+        L.jpet_strip_reference_fp64.argtypes = [C.POINTER(Geom), vp, C.c_int64, vp, vp, C.c_int32,
+                                                C.POINTER(C.c_int64), C.POINTER(C.c_int64), vp]
         L.jpet_strip_run.argtypes = [C.POINTER(Geom), C.POINTER(Opts), vp, C.c_int64, vp, C.c_int,
                                      C.c_int, OUTPUT_FN, PROGRESS_FN, vp, C.c_char_p, C.c_size_t]
         for name in EXPORTED:
@@ -270,6 +273,28 @@ def generate(regions, n: int, radius: float, length: float, sigma_z: float, sigm
     """As generate_device, copied to a host float32[k, 3] array."""
     return generate_device(regions, n, radius, length, sigma_z, sigma_dl, seed, detected,
                            additive, device).cpu().numpy()
+
+
+def reference_fp64(geom: Geometry, events, n_iterations: int, rho=None, device: int = 0):
+    """The reference iteration at double on the GPU.  events: float32[n, 3]
+    (host array or CUDA tensor).  Returns (float64[n_y, n_z] image, counters)."""
+    import torch
+
+    dev = f"cuda:{device}"
+    ev = events if (hasattr(events, "is_cuda") and events.is_cuda) else \
+        torch.from_numpy(np.ascontiguousarray(events, np.float32).reshape(-1, 3))
+    ev = ev.to(dev).contiguous()
+    r = torch.ones((geom.n_y, geom.n_z), dtype=torch.float64, device=dev) if rho is None else \
+        torch.as_tensor(np.asarray(rho, np.float64)).to(dev).contiguous()
+    work = torch.empty_like(r)
+    calls, contrib = C.c_int64(0), C.c_int64(0)
+    g = geom.c()
+    with torch.cuda.device(device):
+        stream = torch.cuda.current_stream().cuda_stream
+        _check(lib().jpet_strip_reference_fp64(C.byref(g), ev.data_ptr(), ev.shape[0],
+                                               r.data_ptr(), work.data_ptr(), n_iterations,
+                                               C.byref(calls), C.byref(contrib), stream))
+    return r.cpu().numpy(), {"n_kernel_calls": calls.value, "n_contributing": contrib.value}
 
 
 class StripBatch:

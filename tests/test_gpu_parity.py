@@ -322,3 +322,23 @@ def test_precision_mode_argument_checks():
         capi.StripReconstruction(g, precision=capi.PRECISION_COMPENSATED,
                                  variant=capi.VARIANT_EXACT)
     assert e.value.code == capi.JPET_ERR_UNSUPPORTED
+
+
+def test_fp64_reference_iteration_matches_fp64_oracle(golden):
+    """jpet_strip_reference_fp64 is the reference template at double: it matches
+    the FP64 oracle (and so the reference's own double instantiation) to
+    summation-order rounding, with the same counters."""
+    manifest, load = golden
+    cg, og = _geoms(manifest["c1"])
+    ev = load("c1_events.npy")
+    got, cnt = capi.reference_fp64(cg, ev, 3)
+    want = load("c1_fp64_it03.npy")
+    assert rel_l2(got, want) < 1e-12
+    _, st = O.mlem_f(og, ev, 1, threads=4)
+    assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
+    # and on the cropped 2 mm case (clamped boxes) against the oracle at double
+    cg2, og2 = _geoms(manifest["crop"])
+    ev2 = load("crop_events.npy")
+    got2, _ = capi.reference_fp64(cg2, ev2, 2)
+    want2 = O.mlem_d(og2, ev2, 2, threads=4)
+    assert rel_l2(got2, want2) < 1e-12
