@@ -73,6 +73,19 @@ def parse():
     return p.parse_args()
 
 
+def replica_value(local_ms, n_events, steps, world, device="cpu"):
+    """Whole-job throughput of N independent replicas: every rank processed
+    n_events per step; the job takes as long as the slowest rank (max over
+    ranks of the timed region).  Returns (max_ms, event-iterations/s)."""
+    import torch
+
+    t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    max_ms = float(t.item())
+    return max_ms, world * n_events * steps / (max_ms * 1e-3)
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -81,7 +94,7 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -94,7 +107,7 @@ class ClockSampler:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(device), f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
                 stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
@@ -255,12 +268,8 @@ def gb300_arm(args, wl, world, rank, local):
     torch.cuda.synchronize()
     clk = clocks.stop()
     per_step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = starts[0].elapsed_time(ends[-1])
-    t_max = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t_max, op=torch.distributed.ReduceOp.MAX)
-    total_ms = float(t_max.item())
-    value = world * n_events * args.steps / (total_ms * 1e-3)
+    total_ms, value = replica_value(starts[0].elapsed_time(ends[-1]), n_events, args.steps,
+                                    world, device="cuda")
     kernel_ms = statistics.mean(per_step_ms)
     evals_per_s = evals_per_iter / (kernel_ms * 1e-3)
 

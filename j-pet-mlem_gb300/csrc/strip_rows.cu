@@ -279,7 +279,9 @@ __device__ __forceinline__ void rows_chunk(
           const int k0 = 2 * gl + kSweep * s;
           const float2 a = __ffma2_rn(q2, jf[s], __fadd2_rn(p2, cj[s]));
           const float2 r2 = *reinterpret_cast<const float2*>(w_rho + bse + kSweep * s);
-          float2 kr = __fmul2_rn(make_float2(ex2_approx(a.x), ex2_approx(a.y)), r2);
+          // two scalar products: packing the two ex2 results for one FMUL2
+          // would cost register moves
+          float2 kr = make_float2(ex2_approx(a.x) * r2.x, ex2_approx(a.y) * r2.y);
           // only the first pixel of the row can lie before the interval
           kr.x = ((s > 0 || k0 >= lead) && k0 < end) ? kr.x : 0.0f;
           kr.y = (k0 + 1 < end) ? kr.y : 0.0f;
