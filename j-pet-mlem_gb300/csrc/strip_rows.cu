@@ -279,9 +279,7 @@ __device__ __forceinline__ void rows_chunk(
           const int k0 = 2 * gl + kSweep * s;
           const float2 a = __ffma2_rn(q2, jf[s], __fadd2_rn(p2, cj[s]));
           const float2 r2 = *reinterpret_cast<const float2*>(w_rho + bse + kSweep * s);
-          // two scalar products: packing the two ex2 results for one FMUL2
-          // would cost register moves
-          float2 kr = make_float2(ex2_approx(a.x) * r2.x, ex2_approx(a.y) * r2.y);
+          float2 kr = __fmul2_rn(make_float2(ex2_approx(a.x), ex2_approx(a.y)), r2);
           // only the first pixel of the row can lie before the interval
           kr.x = ((s > 0 || k0 >= lead) && k0 < end) ? kr.x : 0.0f;
           kr.y = (k0 + 1 < end) ? kr.y : 0.0f;
@@ -327,8 +325,10 @@ __device__ __forceinline__ void rows_chunk(
     // ---- back-projection into this warp's rows
 #pragma unroll
     for (int j = 0; j < E; ++j) {
+      // events without a positive denominator (or outside the register shape,
+      // or past the chunk's end) carry K rho = 0 in every slot, or inv = 0:
+      // their pass below changes no pixel, so it runs without a branch
       const float inv = __shfl_sync(kFull, inv_l, j);
-      if (!((ok_mask >> j) & 1u)) continue;
       // Branch-free read-modify-write of the pixel pair: the pair is always
       // loaded (inside the window), each pixel stored only if it received a
       // contribution, so no lane writes a pixel outside its event's rows.
