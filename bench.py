@@ -477,7 +477,7 @@ def batch_summary(local, iterations=10, k=64):
         plans = {}
         for i in range(k):
             p = b.plan(i)
-            key = f"shape{p['raster_shape']}x{p['block_threads']}"
+            key = f"shape{p['raster_shape']}x{p['block_threads']}t{p['tile']}"
             plans[key] = plans.get(key, 0) + 1
         out["tuned_plans"] = plans
     out["speedup_tuned_vs_single"] = out["single_handles"]["seconds"] / out["batched_tuned"]["seconds"]

@@ -89,6 +89,7 @@ typedef struct jpet_strip_geom {
 #define JPET_RASTER_4x1x3 4 /* <= 64 rows, <= 23 columns */
 #define JPET_RASTER_4x1x4 5 /* <= 64 rows, <= 31 columns */
 #define JPET_RASTER_4x2x4 6 /* <= 128 rows, <= 31 columns */
+#define JPET_RASTER_2x1x6 7 /* <= 64 rows, <= 23 columns, 2 lanes per row */
 
 typedef struct jpet_strip_opts {
   int32_t device;       /* CUDA device ordinal (-D / --cuda-device) */
@@ -263,7 +264,7 @@ typedef struct jpet_strip_batch_plan {
   double tuned_ms_per_iteration; /* best time on the tuning prefix, -1 = not timed */
   int64_t tuned_events;          /* events of the tuning prefix */
   int32_t candidates;            /* plans timed for this instance (0 = cached plan) */
-  int32_t reserved;
+  int32_t tile;                  /* square tile side in pixels (0 = from the window budget) */
 } jpet_strip_batch_plan;
 
 /* opts (NULL = defaults) apply to every instance; device = opts->device. */
@@ -278,10 +279,11 @@ int jpet_strip_batch_instance(jpet_strip_batch_t* b, int32_t i, jpet_strip_t** h
 int jpet_strip_batch_set_events(jpet_strip_batch_t* b, int32_t i, const float* aos, int64_t n,
                                 int32_t on_device);
 /* Autotuner: for every instance, times its automatic register shape and the
- * next larger one with 128- and 256-thread CTAs on the first max_tune_events
- * events (<= 0: 262144) and keeps the fastest; plans are cached by grid,
- * pixel size, widths and event-count octave.  Re-bins the events with the
- * chosen plan and resets every image to uniform 1. */
+ * next larger one with 128- and 256-thread CTAs and two tile sides (the
+ * largest square tile the CTA's window budget allows, and half of it) on the
+ * first max_tune_events events (<= 0: 262144) and keeps the fastest; plans are
+ * cached by grid, pixel size, widths and event-count octave.  Re-bins the
+ * events with the chosen plan and resets every image to uniform 1. */
 int jpet_strip_batch_tune(jpet_strip_batch_t* b, int64_t max_tune_events);
 int jpet_strip_batch_plan_of(const jpet_strip_batch_t* b, int32_t i, jpet_strip_batch_plan* p);
 /* n iterations of every instance: one graph launch (captured on first use for

@@ -13,7 +13,7 @@
 // so that each handle's image is the latest, and the instance table on the
 // device is rewritten to match.
 //
-// The autotuner times candidate (register shape, CTA size) plans per instance
+// The autotuner times candidate (register shape, CTA size, tile) plans per instance
 // on a prefix of its events with the single-handle iteration and keeps the
 // fastest; plans are cached by geometry, widths and event-count octave, so
 // instances of the same kind are timed once.
@@ -35,8 +35,8 @@ int handle_batch_view(jpet_strip* h, BatchInstance* v, std::string& why);
 int32_t handle_n_chunks(const jpet_strip* h);
 int handle_device(const jpet_strip* h);
 void handle_batch_done(jpet_strip* h, int n);
-int handle_reprepare(jpet_strip* h, int raster_shape, int block_threads, const float* d_zu,
-                     const float* d_zd, const float* d_dl, int64_t n);
+int handle_reprepare(jpet_strip* h, int raster_shape, int block_threads, int tile,
+                     const float* d_zu, const float* d_zd, const float* d_dl, int64_t n);
 const char* handle_error(const jpet_strip* h);
 }  // namespace jpet
 
@@ -84,7 +84,7 @@ struct jpet_strip_batch {
   int32_t max_pix = 0;
   bool built = false;
   std::map<int, cudaGraphExec_t> graphs;
-  std::map<TuneKey, std::pair<int, int>> tune_cache;
+  std::map<TuneKey, std::tuple<int, int, int>> tune_cache;  // shape, CTA threads, tile
 
   int fail(int code, const std::string& m) {
     last_error = m;
@@ -346,55 +346,77 @@ int jpet_strip_batch_tune(jpet_strip_batch_t* b, int64_t max_tune_events) {
                       static_cast<int>(std::lround(gv.g.sigma_dl)), octave};
     const int64_t nt = std::min<int64_t>(r.n, max_tune_events);
     auto hit = b->tune_cache.find(key);
-    int best_shape = 0, best_threads = 128;
+    int best_shape = 0, best_threads = 128, best_tile = 0;
     double best_ms = 1e30;
     int n_cand = 0;
     if (hit != b->tune_cache.end()) {
-      best_shape = hit->second.first;
-      best_threads = hit->second.second;
+      std::tie(best_shape, best_threads, best_tile) = hit->second;
     } else if (nt > 0) {
-      // candidates: the automatic shape and the next larger one, 4- and 8-warp CTAs
-      rc = handle_reprepare(h, JPET_RASTER_AUTO, 128, r.d, r.d + r.n, r.d + 2 * r.n, nt);
-      if (rc != JPET_OK) break;
-      BatchInstance v{};
-      std::string why;
-      handle_batch_view(h, &v, why);
-      const int auto_shape = v.t.rows_shape + 1;  // JPET_RASTER_* numbering
-      std::vector<int> shapes{auto_shape};
-      if (auto_shape < JPET_RASTER_4x2x4) shapes.push_back(auto_shape + 1);
+      // candidates: the automatic register shape and the next larger one, 4- and
+      // 8-warp CTAs, and the automatic square tile of that CTA's window budget or
+      // one of half its side
+      std::vector<int> shapes;
+      {
+        rc = handle_reprepare(h, JPET_RASTER_AUTO, 128, 0, r.d, r.d + r.n, r.d + 2 * r.n, nt);
+        if (rc != JPET_OK) break;
+        BatchInstance v{};
+        std::string why;
+        handle_batch_view(h, &v, why);
+        const int auto_shape = v.t.rows_shape + 1;  // JPET_RASTER_* numbering
+        shapes.push_back(auto_shape);
+        if (auto_shape < JPET_RASTER_4x2x4) shapes.push_back(auto_shape + 1);
+      }
       for (int shape : shapes) {
         for (int threads : {128, 256}) {
-          rc = handle_reprepare(h, shape, threads, r.d, r.d + r.n, r.d + 2 * r.n, nt);
-          if (rc != JPET_OK) break;
-          rc = jpet_strip_iterate(h, 1);  // warm-up
-          if (rc != JPET_OK) break;
-          BATCH_CUDA(b, cudaEventRecord(e0, b->stream), "event");
-          rc = jpet_strip_iterate(h, 3);
-          if (rc != JPET_OK) break;
-          BATCH_CUDA(b, cudaEventRecord(e1, b->stream), "event");
-          BATCH_CUDA(b, cudaEventSynchronize(e1), "event");
-          float ms = 0;
-          BATCH_CUDA(b, cudaEventElapsedTime(&ms, e0, e1), "event");
-          ++n_cand;
-          if (ms / 3 < best_ms) {
-            best_ms = ms / 3;
-            best_shape = shape;
-            best_threads = threads;
+          int auto_tile = 0;
+          for (int tile_pass = 0; tile_pass < 2 && rc == JPET_OK; ++tile_pass) {
+            int tile = 0;
+            if (tile_pass == 1) {
+              tile = auto_tile / 2;
+              if (tile < 8) break;
+            }
+            rc = handle_reprepare(h, shape, threads, tile, r.d, r.d + r.n, r.d + 2 * r.n, nt);
+            if (rc != JPET_OK) break;
+            if (tile_pass == 0) {
+              BatchInstance v{};
+              std::string why;
+              handle_batch_view(h, &v, why);
+              auto_tile = std::min(v.t.tile_w, v.t.tile_h);
+            }
+            rc = jpet_strip_iterate(h, 1);  // warm-up
+            if (rc != JPET_OK) break;
+            BATCH_CUDA(b, cudaEventRecord(e0, b->stream), "event");
+            rc = jpet_strip_iterate(h, 3);
+            if (rc != JPET_OK) break;
+            BATCH_CUDA(b, cudaEventRecord(e1, b->stream), "event");
+            BATCH_CUDA(b, cudaEventSynchronize(e1), "event");
+            float ms = 0;
+            BATCH_CUDA(b, cudaEventElapsedTime(&ms, e0, e1), "event");
+            ++n_cand;
+            if (ms / 3 < best_ms) {
+              best_ms = ms / 3;
+              best_shape = shape;
+              best_threads = threads;
+              best_tile = tile;
+            }
           }
+          if (rc != JPET_OK) break;
         }
         if (rc != JPET_OK) break;
       }
       if (rc != JPET_OK) break;
-      b->tune_cache[key] = {best_shape, best_threads};
+      b->tune_cache[key] = std::make_tuple(best_shape, best_threads, best_tile);
     }
     // the chosen plan on all of the instance's events, from a uniform image
-    rc = handle_reprepare(h, best_shape, best_threads, r.d, r.d + r.n, r.d + 2 * r.n, r.n);
+    rc = handle_reprepare(h, best_shape, best_threads, best_tile, r.d, r.d + r.n, r.d + 2 * r.n,
+                          r.n);
     if (rc != JPET_OK) break;
     std::vector<float> ones(static_cast<size_t>(gv.n_pix), 1.0f);
     rc = jpet_strip_set_image(h, ones.data());
     if (rc != JPET_OK) break;
     b->plan[i].raster_shape = best_shape;
     b->plan[i].block_threads = best_threads;
+    b->plan[i].tile = best_tile;
     b->plan[i].tuned_ms_per_iteration = best_ms < 1e30 ? best_ms : -1.0;
     b->plan[i].tuned_events = nt;
     b->plan[i].candidates = n_cand;

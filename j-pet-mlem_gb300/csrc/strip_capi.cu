@@ -454,10 +454,11 @@ void handle_batch_done(jpet_strip* h, int n) {
   h->counters_valid = true;
 }
 
-int handle_reprepare(jpet_strip* h, int raster_shape, int block_threads, const float* d_zu,
-                     const float* d_zd, const float* d_dl, int64_t n) {
+int handle_reprepare(jpet_strip* h, int raster_shape, int block_threads, int tile,
+                     const float* d_zu, const float* d_zd, const float* d_dl, int64_t n) {
   h->opts.raster_shape = raster_shape;
   h->opts.block_threads = block_threads;
+  h->opts.tile_w = h->opts.tile_h = tile;
   return prepare_events(h, d_zu, d_zd, d_dl, n);
 }
 
@@ -504,7 +505,7 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
     g_create_error = "the row-owned kernel runs 128- or 256-thread CTAs";
     return JPET_ERR_ARGUMENT;
   }
-  if (o.raster_shape < JPET_RASTER_AUTO || o.raster_shape > JPET_RASTER_4x2x4) {
+  if (o.raster_shape < JPET_RASTER_AUTO || o.raster_shape > JPET_RASTER_2x1x6) {
     g_create_error = "unknown rasterisation shape";
     return JPET_ERR_ARGUMENT;
   }

@@ -62,6 +62,7 @@ enum RowsShape : int32_t {
   kRowsShape4x1x3 = 3,  // <= 64 rows, <= 23 columns
   kRowsShape4x1x4 = 4,  // <= 64 rows, <= 31 columns
   kRowsShape4x2x4 = 5,  // <= 128 rows, <= 31 columns
+  kRowsShape2x1x6 = 6,  // <= 64 rows (4-warp CTAs; 128 with 8), <= 23 columns
 };
 
 // Constants of the fast evaluation: the Gaussian kernel written as

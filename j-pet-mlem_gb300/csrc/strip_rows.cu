@@ -572,6 +572,9 @@ cudaError_t batch_rows_shape(int shape, int op, size_t smem, int grid, int* bps,
     case kRowsShape4x1x4:
       return batch_rows_dispatch<NW, 4, 64, 4>(op, smem, grid, bps, insts, items, n_items, next,
                                                parity, s);
+    case kRowsShape2x1x6:
+      return batch_rows_dispatch<NW, 2, 64, 6>(op, smem, grid, bps, insts, items, n_items, next,
+                                               parity, s);
     default:
       return batch_rows_dispatch<NW, 4, 128, 4>(op, smem, grid, bps, insts, items, n_items, next,
                                                 parity, s);
@@ -642,6 +645,9 @@ cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Til
     case kRowsShape4x1x4:
       return launch_rows_shape<4, 64, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho,
                                          out, out64, counters, precision, seed, s);
+    case kRowsShape2x1x6:
+      return launch_rows_shape<2, 64, 6>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho,
+                                         out, out64, counters, precision, seed, s);
     default:
       return launch_rows_shape<4, 128, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho,
                                           out, out64, counters, precision, seed, s);
@@ -650,10 +656,10 @@ cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Til
 
 size_t rows_smem_bytes(const Tiling& t, int threads, int rows_shape) {
   const int nw = threads == 256 ? 8 : 4;
-  static const int rows_of[] = {32, 32, 64, 64, 64, 128};
-  static const int g_of[] = {8, 8, 4, 4, 4, 4};
-  static const int sw_of[] = {1, 2, 2, 3, 4, 4};
-  const int k = (rows_shape >= 0 && rows_shape <= kRowsShape4x2x4) ? rows_shape : kRowsShape4x2x4;
+  static const int rows_of[] = {32, 32, 64, 64, 64, 128, 64};
+  static const int g_of[] = {8, 8, 4, 4, 4, 4, 2};
+  static const int sw_of[] = {1, 2, 2, 3, 4, 4, 6};
+  const int k = (rows_shape >= 0 && rows_shape <= kRowsShape2x1x6) ? rows_shape : kRowsShape4x2x4;
   const int pass = nw * (32 / g_of[k]);
   const int rs = (rows_of[k] + pass - 1) / pass;
   const int e = (rs * sw_of[k] <= 4) ? 8 : (rs * sw_of[k] <= 8 ? 4 : 2);

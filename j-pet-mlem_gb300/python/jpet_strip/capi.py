@@ -36,7 +36,8 @@ VARIANT_FAST = 0
 VARIANT_EXACT = 1
 VARIANT_WARP = 2
 RASTER_AUTO = 0
-RASTER_SHAPES = {"8x1x1": 1, "8x1x2": 2, "4x1x2": 3, "4x1x3": 4, "4x1x4": 5, "4x2x4": 6}
+RASTER_SHAPES = {"8x1x1": 1, "8x1x2": 2, "4x1x2": 3, "4x1x3": 4, "4x1x4": 5, "4x2x4": 6,
+                 "2x1x6": 7}
 
 # every symbol include/jpet_strip.h declares
 EXPORTED = [
@@ -112,7 +113,7 @@ class BatchPlan(C.Structure):
         ("tuned_ms_per_iteration", C.c_double),
         ("tuned_events", C.c_int64),
         ("candidates", C.c_int32),
-        ("reserved", C.c_int32),
+        ("tile", C.c_int32),
     ]
 
 
@@ -350,7 +351,7 @@ class StripBatch:
     def plan(self, i: int) -> dict:
         p = BatchPlan()
         self._ck(lib().jpet_strip_batch_plan_of(self._b, i, C.byref(p)))
-        return {f: getattr(p, f) for f, _ in BatchPlan._fields_ if f != "reserved"}
+        return {f: getattr(p, f) for f, _ in BatchPlan._fields_}
 
     def iterate(self, n: int = 1):
         self._ck(lib().jpet_strip_batch_iterate(self._b, n))
