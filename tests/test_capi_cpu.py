@@ -104,3 +104,27 @@ def phantom_ellipse():
     from jpet_strip import phantom
 
     return phantom.Ellipse(0.0, 0.0, 100.0, 80.0, 10.0, 1.0)
+
+
+def test_binding_fails_loudly_without_the_library(monkeypatch, tmp_path):
+    """The product has no CPU fallback: with libjpet_strip.so missing the
+    binding raises instead of computing anything."""
+    monkeypatch.setattr(capi, "LIB_PATH", str(tmp_path / "missing.so"))
+    monkeypatch.setattr(capi, "_lib", None)
+    with pytest.raises(ImportError):
+        capi.lib()
+    with pytest.raises(ImportError):
+        capi.StripReconstruction(capi.Geometry(450, 1000, 90, 100, 10, 10, 42))
+
+
+def test_batch_create_rejects_unsupported_options_without_device():
+    import ctypes as C
+
+    L = capi.lib()
+    g = capi.Geometry(450, 1000, 90, 100, 10, 10, 42).c()
+    arr = (capi.Geom * 1)(g)
+    b = C.c_void_p()
+    o = capi.make_opts(precision=capi.PRECISION_FIXED)
+    assert L.jpet_strip_batch_create(1, arr, C.byref(o), C.byref(b)) == capi.JPET_ERR_UNSUPPORTED
+    assert L.jpet_strip_batch_create(0, arr, None, C.byref(b)) == capi.JPET_ERR_ARGUMENT
+    assert L.jpet_strip_batch_destroy(None) == capi.JPET_OK
