@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--no-batch", action="store_true",
                    help="skip the batched form (64 reconstructions per graph launch)")
     p.add_argument("--batch-instances", type=int, default=64)
+    p.add_argument("--no-adjoint", action="store_true",
+                   help="skip the differentiable form (adjoint throughput and calibration)")
     p.add_argument("--sample-events", type=int, default=1_000_000,
                    help="events of the FP64-oracle prefix in the precision report")
     p.add_argument("--precision-report", action="store_true",
@@ -333,6 +335,12 @@ def gb300_arm(args, wl, world, rank, local):
             batched = batch_summary(local, k=args.batch_instances)
         except Exception as exc:  # reported, the headline line still prints
             batched = {"error": f"{type(exc).__name__}: {exc}"}
+    adjoint = None
+    if not args.no_adjoint:
+        try:
+            adjoint = adjoint_summary(local)
+        except Exception as exc:  # reported, the headline line still prints
+            adjoint = {"error": f"{type(exc).__name__}: {exc}"}
     hbm, hbm_kind = hbm_peak()
     roofline = None
     if peaks:
@@ -384,6 +392,7 @@ def gb300_arm(args, wl, world, rank, local):
         "counters": counters,
         "kernel_ms_per_iteration": kernel_ms,
         "batched": batched,
+        "adjoint": adjoint,
     }
     print(json.dumps(line), flush=True)
 
@@ -453,9 +462,19 @@ def batch_summary(local, iterations=10, k=64):
         for i, ev in enumerate(events):
             b.set_events(i, ev)
         b.iterate(1)  # one batched iteration from the uniform image
+        batch_one = [b.instance(i).rho.astype(np.float64) for i in range(k)]
         out["max_rel_l2_vs_single_handles_1_iteration"] = max(
-            float(np.linalg.norm(b.instance(i).rho.astype(np.float64) - single_one[i])
+            float(np.linalg.norm(batch_one[i] - single_one[i])
                   / max(np.linalg.norm(single_one[i]), 1e-30)) for i in range(k))
+        # accuracy against FP64 after one iteration (the reference iteration at
+        # double on the GPU), batched and single-handle, on every instance
+        e_b, e_s = [], []
+        for i in range(k):
+            f64, _ = capi.reference_fp64(geoms[i], events[i], 1, device=local)
+            nrm = max(np.linalg.norm(f64), 1e-30)
+            e_b.append(float(np.linalg.norm(batch_one[i] - f64) / nrm))
+            e_s.append(float(np.linalg.norm(single_one[i] - f64) / nrm))
+        out["max_rel_l2_vs_fp64_1_iteration"] = {"batched": max(e_b), "single_handles": max(e_s)}
         for label in ("batched", "batched_tuned"):
             if label == "batched_tuned":
                 t0 = time.perf_counter()
@@ -482,6 +501,44 @@ def batch_summary(local, iterations=10, k=64):
         out["tuned_plans"] = plans
     out["speedup_tuned_vs_single"] = out["single_handles"]["seconds"] / out["batched_tuned"]["seconds"]
     return out
+
+
+def adjoint_summary(local, n_events=5_000_000):
+    """Differentiable form: 5e6 events of a centred point source simulated with
+    sigma (10, 42) on the 2 mm grid.  Times one loss + gradient evaluation
+    (dL/drho image and dL/dsigma) at the mis-specified widths (14, 55), then
+    recalibrates the widths from (14, 55) by gradient descent with the source
+    image known."""
+    import numpy as np
+    import torch
+
+    from jpet_strip import capi, phantom
+    from jpet_strip.autograd import calibrate_sigma
+
+    geom = capi.Geometry(450.0, 1000.0, 450, 500, 2.0, 14.0, 55.0)
+    ev = capi.generate(phantom.point_source(), n_events, 450.0, 1000.0, 10.0, 42.0, seed=3,
+                       device=local)
+    img = phantom.point_image(450, 500, 2.0, [(-1.0, -1.0)]) * np.float32(n_events)
+    rho = torch.from_numpy(img).cuda(local)
+    grad = torch.empty_like(rho)
+    with capi.StripReconstruction(geom, device=local) as rec:
+        rec.set_events(ev)
+        rec.nll_grad(14.0, 55.0, rho.data_ptr(), None, grad.data_ptr())  # warm-up
+        torch.cuda.synchronize()
+        reps = 5
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            loss, gs, skipped = rec.nll_grad(14.0, 55.0, rho.data_ptr(), None, grad.data_ptr())
+        dt = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    sigma, hist = calibrate_sigma(geom, ev, img, (14.0, 55.0), device=local)
+    cal_s = time.perf_counter() - t0
+    return {"events": n_events, "grid": "500x450", "pixel_mm": 2.0,
+            "true_sigma": [10.0, 42.0], "start_sigma": [14.0, 55.0],
+            "loss_and_gradient_ms": 1e3 * dt, "events_per_s": n_events / dt,
+            "recovered_sigma": [float(sigma[0]), float(sigma[1])],
+            "calibration_steps": len(hist), "calibration_seconds": cal_s,
+            "within_0p5_mm": bool(abs(sigma[0] - 10.0) < 0.5 and abs(sigma[1] - 42.0) < 0.5)}
 
 
 def precision_report(args, local):

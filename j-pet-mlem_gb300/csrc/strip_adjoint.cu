@@ -25,7 +25,8 @@
 //
 // One warp per event; each row's exact in-ellipse interval is found with the
 // same search as the MLEM row tables (row_interval), so the support is exactly
-// the reference's.  For the events of the tiled chunks the rho window and a
+// the reference's.  The rows' constants are set up 32 at a time, one row per
+// lane, and broadcast to the warp for the row's pixels.  For the events of the tiled chunks the rho window and a
 // gradient window live in shared memory (as in the MLEM kernel); events whose
 // box exceeds the windows use the global image.  Per-event log-likelihood and
 // sigma-derivative terms are reduced in FP64 per CTA.
@@ -95,34 +96,50 @@ __device__ __forceinline__ void nll_event(const DevGeom& g, const NllConst& k, f
       }
       inv = static_cast<float>(1.0 / dd);
     }
-    for (int ri = 0; ri < nrows; ++ri) {
-      const int iy = box.y + ri;
-      int first;
-      const int w = row_interval(g, A, B, C, z, y, tn, sec, box.x, box.z, iy, first);
-      if (w == 0) continue;
-      const float py = g.tl_y_half_h - static_cast<float>(iy) * g.pixel_height;
-      const float dy = py - y;
-      const float pa = pa_c * (py * py + g.radius * g.radius), qa = qa_c * py * py;
-      const float ama = pa * k.ipz + qa * k.ipd;
-      const double dyd = dy;
-      const float row_arg = static_cast<float>(
-          -0.5 * kNllLog2e * log1p(qq * dyd * (static_cast<double>(py) + y)) +
-          kdl_sec2 * dyd * dyd);
-      const float cz = k.inv_ipz - 0.5f * pa / ama;
-      const float cdl = k.half_inv_ipd - 0.5f * qa / ama - 2.0f * sec2 * dy * dy;
-      const float u_row = g.tl_z_half_w - z - dy * tn;
-      for (int j = lane; j < w; j += 32) {
-        const int col = first + j;
-        const float u = fmaf(static_cast<float>(col), g.pixel_width, u_row);
-        const float kv = exp2f(fmaf(k.kz * u, u, fmaf(k.kz_lo * u, u, row_arg)));
-        const int wi = wv.index(iy, col);
-        if (pass == 0) {
-          const float kr = kv * wv.rho[wi];
-          den += kr;
-          dz += kr * (cz - u * u);
-          ddl += kr * cdl;
-        } else {
-          atomicAdd(&wv.grad[wi], -kv * inv);
+    // rows in groups of 32: lane l sets up row rb + l (exact interval, FP64 row
+    // term), then the warp sweeps the group's rows one by one with the
+    // constants broadcast from their lanes
+    for (int rb = 0; rb < nrows; rb += 32) {
+      const int ri = rb + lane;
+      int first = 0, w = 0;
+      float row_arg = 0.0f, cz = 0.0f, cdl = 0.0f, u_row = 0.0f;
+      if (ri < nrows) {
+        const int iy = box.y + ri;
+        w = row_interval(g, A, B, C, z, y, tn, sec, box.x, box.z, iy, first);
+        const float py = g.tl_y_half_h - static_cast<float>(iy) * g.pixel_height;
+        const float dy = py - y;
+        const float pa = pa_c * (py * py + g.radius * g.radius), qa = qa_c * py * py;
+        const float ama = pa * k.ipz + qa * k.ipd;
+        const double dyd = dy;
+        row_arg = static_cast<float>(-0.5 * kNllLog2e * log1p(qq * dyd * (static_cast<double>(py) + y)) +
+                                     kdl_sec2 * dyd * dyd);
+        cz = k.inv_ipz - 0.5f * pa / ama;
+        cdl = k.half_inv_ipd - 0.5f * qa / ama - 2.0f * sec2 * dy * dy;
+        u_row = g.tl_z_half_w - z - dy * tn;
+      }
+      const int n_group = min(32, nrows - rb);
+      for (int r = 0; r < n_group; ++r) {
+        const int wr = __shfl_sync(kFull, w, r);
+        if (wr == 0) continue;
+        const int fr = __shfl_sync(kFull, first, r);
+        const float ra = __shfl_sync(kFull, row_arg, r);
+        const float czr = __shfl_sync(kFull, cz, r);
+        const float cdr = __shfl_sync(kFull, cdl, r);
+        const float ur = __shfl_sync(kFull, u_row, r);
+        const int iy = box.y + rb + r;
+        for (int j = lane; j < wr; j += 32) {
+          const int col = fr + j;
+          const float u = fmaf(static_cast<float>(col), g.pixel_width, ur);
+          const float kv = exp2f(fmaf(k.kz * u, u, fmaf(k.kz_lo * u, u, ra)));
+          const int wi = wv.index(iy, col);
+          if (pass == 0) {
+            const float kr = kv * wv.rho[wi];
+            den += kr;
+            dz += kr * (czr - u * u);
+            ddl += kr * cdr;
+          } else {
+            atomicAdd(&wv.grad[wi], -kv * inv);
+          }
         }
       }
     }

@@ -145,7 +145,7 @@ int run(int argc, char* argv[]) {
     throw "at least one input phantom description expected, consult --help";
   }
   for (const char* opt : {"full", "no-responses", "tan-bins", "kernel-point"})
-    if (cl.exist(opt)) throw std::string("--") + opt + " is not supported by this build";
+    if (cl.exist(opt)) throw std::string("--") + opt + " is not supported by this tool";
 
   const uint64_t n = cl.get_size("n-emissions");
   const int verbose = cl.count("verbose");

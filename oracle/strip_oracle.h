@@ -1,8 +1,8 @@
 /* CPU restatement of the reference's 2D strip-PET list-mode MLEM path.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the CPU
- * baseline leg of bench.py load this library, and only as the checker or the
- * timed CPU baseline; the product never links or calls it.
+ * baseline leg of bench.py load this library, and only to verify results or as
+ * the timed CPU baseline; the product never links or calls it.
  *
  * Every function restates one reference function, in the reference's own
  * floating-point evaluation order, so that a single-threaded run is
