@@ -76,7 +76,9 @@ struct jpet_strip {
   DevBuf<int32_t> ev_key, tile_count, tile_offset, tile_cursor, hist, small;
   DevBuf<Chunk> chunks;
   DevBuf<uint16_t> row_table;
-  DevBuf<float2> row_pq;  // per-row exponent coefficients of the row-owned kernel
+  DevBuf<float2> row_pq;     // per-row exponent coefficients of the row-owned kernel
+  DevBuf<uint32_t> row_pk;   // per-row packed window offset / parity / width
+  DevBuf<uint32_t> ev_pk;    // per-event packed window row / box rows / fits
   FastConst fc{};
   bool use_fast = false;
   bool counters_valid = false;
@@ -363,8 +365,12 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
     if (h->opts.variant == JPET_VARIANT_FAST) {
       JPET_CUDA(h, h->row_pq.alloc(static_cast<size_t>(acc) * t.row_stride),
                 "cudaMalloc(row coefficients)");
+      JPET_CUDA(h, h->row_pk.alloc(static_cast<size_t>(acc) * t.row_stride),
+                "cudaMalloc(row words)");
+      JPET_CUDA(h, h->ev_pk.alloc(static_cast<size_t>(acc)), "cudaMalloc(event words)");
       JPET_CUDA(h, launch_row_coefficients(h->g, h->fc, t, acc, h->sorted_geom.p,
-                                           h->sorted_box.p, h->row_table.p, h->row_pq.p, s),
+                                           h->sorted_box.p, h->row_table.p, h->row_pq.p,
+                                           h->row_pk.p, h->ev_pk.p, s),
                 "row coefficient launch");
     }
     JPET_CUDA(h, cudaMemcpyAsync(&h->table_kernel_calls, h->box_pixels.p,
@@ -432,7 +438,8 @@ int handle_batch_view(jpet_strip* h, BatchInstance* v, std::string& why) {
   v->chunks = h->chunks.p;
   v->ev_geom = h->sorted_geom.p;
   v->ev_box = h->sorted_box.p;
-  v->rows = h->row_table.p;
+  v->ev_pk = h->ev_pk.p;
+  v->rows = h->row_pk.p;
   v->pq = h->row_pq.p;
   v->img[0] = h->rho.p;
   v->img[1] = h->out.p;
@@ -601,6 +608,8 @@ int jpet_strip_destroy(jpet_strip_t* h) {
   h->chunks.release();
   h->row_table.release();
   h->row_pq.release();
+  h->row_pk.release();
+  h->ev_pk.release();
   h->box_pixels.release();
   h->nll_acc.release();
   h->nll_grad_tmp.release();
@@ -694,9 +703,9 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
                   "iteration kernel launch");
       } else {
         JPET_CUDA(h, launch_iterate_rows(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
-                                         h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
-                                         h->row_pq.p, h->rho.p, h->out.p, h->out64.p,
-                                         h->counters.p, prec, seed, s),
+                                         h->sorted_geom.p, h->sorted_box.p, h->ev_pk.p,
+                                         h->row_pk.p, h->row_pq.p, h->rho.p, h->out.p,
+                                         h->out64.p, h->counters.p, prec, seed, s),
                   "iteration kernel launch");
       }
     } else {

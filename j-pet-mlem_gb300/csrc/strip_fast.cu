@@ -422,17 +422,22 @@ cudaError_t launch_row_tables(const DevGeom& g, const Tiling& t, int32_t n_event
   return cudaGetLastError();
 }
 
-// Iteration-invariant exponent coefficients of every (event, row) for the
-// row-owned kernel: with the window origin ox of the event's tile (rounded down
+// Iteration-invariant data of every (event, row) for the row-owned kernel: the
+// packed row word (window offset of the sweep start, interval parity, width),
+// the packed event word (window row of the box top, box rows, whether the box
+// fits the register shape), and the exponent coefficients: with the window origin ox of the event's tile (rounded down
 // to an even column, as the kernel's window) and a = the row's first column
 // rounded down to even, the exponent of the j-th pixel from a is
 // p + q j + kz pw^2 j^2 (the form of fast_event's phase A).
 __global__ void __launch_bounds__(256) row_coeff_kernel(DevGeom g, FastConst fc, Tiling t,
-                                                        int32_t n, int32_t stride,
+                                                        int32_t n, int32_t stride, int pitch,
+                                                        int shape_rows, int shape_cols,
                                                         const float4* __restrict__ ev_geom,
                                                         const short4* __restrict__ ev_box,
                                                         const uint16_t* __restrict__ rows,
-                                                        float2* __restrict__ pq) {
+                                                        float2* __restrict__ pq,
+                                                        uint32_t* __restrict__ row_pk,
+                                                        uint32_t* __restrict__ ev_pk) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -448,12 +453,23 @@ __global__ void __launch_bounds__(256) row_coeff_kernel(DevGeom g, FastConst fc,
     const float lref = 0.5f * lg2_approx(fmaf(Q, y * y, P));
     const float u_base = g.tl_z_half_w - z;
     const int ox = ((box.x / t.tile_w) * t.tile_w) & ~1;
+    const int r0 = box.y - (box.y / t.tile_h) * t.tile_h;  // window row of the box top
     const int col0 = box.x - ox;
     const int nrows = box.w - box.y;
+    if (lane == 0) {
+      const int maxw = rows[static_cast<size_t>(e) * stride + stride - 1];
+      const bool fits = nrows <= shape_rows && maxw + 1 <= shape_cols;
+      ev_pk[e] = static_cast<uint32_t>(r0) | (static_cast<uint32_t>(nrows) << 12) |
+                 (fits ? 0x80000000u : 0u);
+      row_pk[static_cast<size_t>(e) * stride + stride - 1] = static_cast<uint32_t>(maxw);
+    }
     for (int ri = lane; ri < nrows; ri += 32) {
       const uint32_t en = rows[static_cast<size_t>(e) * stride + ri];
       const int lo = col0 + static_cast<int>(en & 255u);
       const int a_off = lo & ~1;
+      row_pk[static_cast<size_t>(e) * stride + ri] =
+          static_cast<uint32_t>((r0 + ri) * pitch + a_off) | static_cast<uint32_t>(lo & 1) |
+          ((en >> 8) << 24);
       const float py = g.tl_y_half_h - static_cast<float>(box.y + ri) * g.pixel_height;
       const float dy = py - y;
       const float lf = lref - 0.5f * lg2_approx(fmaf(Q, py * py, P));
@@ -467,12 +483,16 @@ __global__ void __launch_bounds__(256) row_coeff_kernel(DevGeom g, FastConst fc,
 cudaError_t launch_row_coefficients(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                     int32_t n_events, const float4* ev_geom,
                                     const short4* ev_box, const uint16_t* rows, float2* pq,
-                                    cudaStream_t s) {
+                                    uint32_t* row_pk, uint32_t* ev_pk, cudaStream_t s) {
   if (n_events <= 0) return cudaSuccess;
+  if (static_cast<int64_t>(t.win_h) * fast_pitch(t) >= (1 << 24) || t.win_h >= 4096)
+    return cudaErrorInvalidValue;  // packed offsets hold 24 bits, window rows 12
   int blocks = (n_events + 7) / 8;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  row_coeff_kernel<<<blocks, 256, 0, s>>>(g, fc, t, n_events, t.row_stride, ev_geom, ev_box,
-                                          rows, pq);
+  row_coeff_kernel<<<blocks, 256, 0, s>>>(g, fc, t, n_events, t.row_stride, fast_pitch(t),
+                                          rows_shape_rows(t.rows_shape),
+                                          rows_sweep_cols(t.rows_shape), ev_geom, ev_box, rows,
+                                          pq, row_pk, ev_pk);
   return cudaGetLastError();
 }
 

@@ -121,17 +121,24 @@ enum FastPrecision : int32_t {
   kPrecisionCompensatedDen64 = 2,
   kPrecisionFixed = 3,
 };
+// Per (event, row): exponent coefficients (p, q) and the packed row word
+// (window offset of the row's even start column | interval parity | width << 24;
+// the last entry of an event: its widest row); per event: the packed event word
+// (window row of the box top | box rows << 12 | fits-the-shape << 31).
 cudaError_t launch_row_coefficients(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                     int32_t n_events, const float4* ev_geom,
                                     const short4* ev_box, const uint16_t* rows, float2* pq,
-                                    cudaStream_t s);
+                                    uint32_t* row_pk, uint32_t* ev_pk, cudaStream_t s);
 int rows_shape_for(int rows999, int width);
+// rows and columns (2 G SW) an event may span in a register shape
+int rows_shape_rows(int rows_shape);
+int rows_sweep_cols(int rows_shape);
 cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
-                                const short4* ev_box, const uint16_t* rows, const float2* pq,
-                                const float* rho, float* out, double* out64,
-                                DevCounters* counters, int precision, uint32_t seed,
-                                cudaStream_t s);
+                                const short4* ev_box, const uint32_t* ev_pk,
+                                const uint32_t* rows, const float2* pq, const float* rho,
+                                float* out, double* out64, DevCounters* counters,
+                                int precision, uint32_t seed, cudaStream_t s);
 cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint16_t* rows, const float* rho,
@@ -176,7 +183,8 @@ struct BatchInstance {
   const Chunk* chunks;
   const float4* ev_geom;
   const short4* ev_box;
-  const uint16_t* rows;
+  const uint32_t* ev_pk;
+  const uint32_t* rows;
   const float2* pq;
   float* img[2];  // iteration k reads img[k & 1] and writes img[(k + 1) & 1]
   DevCounters* counters;

@@ -46,12 +46,6 @@ __device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
   return __fadd2_rn(a, make_float2(-b.x, -b.y));
 }
 
-__device__ __forceinline__ void cp_async8(void* dst, const void* src, bool valid) {
-  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
-  const int n = valid ? 8 : 0;
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(n)
-               : "memory");
-}
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
   const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
   const int n = valid ? 16 : 0;
@@ -65,12 +59,21 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
-// Staging buffer of one batch: E boxes, E row tables (u16) and E rows of
-// exponent coefficients (float2), each 16-byte aligned.
-__host__ __device__ inline int rows_stage_tab(int e) { return e * 8; }
-__host__ __device__ inline int rows_stage_pq(int e, int stride) { return e * 8 + e * stride * 2; }
+// Staging buffer of one batch: E packed event words, E packed row tables and E
+// rows of exponent coefficients (float2), each part 16-byte aligned.
+__host__ __device__ inline int rows_stage_tab(int e) { return (e * 4 + 15) & ~15; }
+__host__ __device__ inline int rows_stage_pq(int e, int stride) {
+  return rows_stage_tab(e) + e * stride * 4;
+}
 __host__ __device__ inline int rows_stage_bytes(int e, int stride) {
   return (rows_stage_pq(e, stride) + e * stride * 8 + 15) & ~15;
+}
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, bool valid) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  const int n = valid ? 4 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(n)
+               : "memory");
 }
 
 // Sum over the 32 lanes of E per-lane values, transposed: afterwards lane l
@@ -142,9 +145,9 @@ template <int NW, int G, int RS, int SW, int E, int ACC, bool DEN64>
 __device__ __forceinline__ void rows_chunk(
     const DevGeom& g, const FastConst& fc, const Tiling& t, const Chunk c,
     const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
-    const uint16_t* __restrict__ rows, const float2* __restrict__ row_pq,
-    const float* __restrict__ rho, float* __restrict__ out, double* __restrict__ out64,
-    DevCounters* counters, uint32_t seed) {
+    const uint32_t* __restrict__ ev_pk, const uint32_t* __restrict__ rows,
+    const float2* __restrict__ row_pq, const float* __restrict__ rho, float* __restrict__ out,
+    double* __restrict__ out64, DevCounters* counters, uint32_t seed) {
   constexpr int kRowsPerWarp = 32 / G;       // rows of one warp step
   constexpr int kPass = NW * kRowsPerWarp;   // event rows covered by one step of all warps
   constexpr int kSweep = 2 * G;              // columns per sweep
@@ -170,11 +173,11 @@ __device__ __forceinline__ void rows_chunk(
   const int gid = lane / G, gl = lane % G;
   const int n_batches = (c.count + E - 1) / E;
 
-  auto stage_box = [&](int buf) {
-    return reinterpret_cast<short4*>(stage0 + buf * stage_bytes);
+  auto stage_ev = [&](int buf) {
+    return reinterpret_cast<uint32_t*>(stage0 + buf * stage_bytes);
   };
   auto stage_tab = [&](int buf) {
-    return reinterpret_cast<uint16_t*>(stage0 + buf * stage_bytes + rows_stage_tab(E));
+    return reinterpret_cast<uint32_t*>(stage0 + buf * stage_bytes + rows_stage_tab(E));
   };
   auto stage_pq = [&](int buf) {
     return reinterpret_cast<float2*>(stage0 + buf * stage_bytes + rows_stage_pq(E, stride));
@@ -184,18 +187,18 @@ __device__ __forceinline__ void rows_chunk(
     const int tid = threadIdx.x;
     if (tid < E) {
       const bool v = e0 + tid < c.count;
-      cp_async8(stage_box(buf) + tid, ev_box + c.start + min(e0 + tid, c.count - 1), v);
+      cp_async4(stage_ev(buf) + tid, ev_pk + c.start + min(e0 + tid, c.count - 1), v);
     }
-    const int n_tab = E * stride / 8;  // 16-byte pieces of the E row tables
+    const int n_tab = E * stride / 4;  // 16-byte pieces of the E row tables
     const int n_pq = E * stride / 2;   // 16-byte pieces of the E coefficient rows
-    uint16_t* st = stage_tab(buf);
+    uint32_t* st = stage_tab(buf);
     float2* sp = stage_pq(buf);
     for (int k = tid; k < n_tab + n_pq; k += NW * 32) {
       if (k < n_tab) {
-        const int ek = (k * 8) / stride;
+        const int ek = (k * 4) / stride;
         const bool v = e0 + ek < c.count;
         const size_t src = static_cast<size_t>(c.start + min(e0 + ek, c.count - 1)) * stride;
-        cp_async16(st + k * 8, rows + src + (k * 8 - ek * stride), v);
+        cp_async16(st + k * 4, rows + src + (k * 4 - ek * stride), v);
       } else {
         const int kk = k - n_tab;
         const int ek = (kk * 2) / stride;
@@ -238,8 +241,8 @@ __device__ __forceinline__ void rows_chunk(
   for (int b = 0; b < n_batches; ++b) {
     const int buf = b & 1;
     if (b + 1 < n_batches) issue_stage(b + 1, buf ^ 1);
-    const short4* sb = stage_box(buf);
-    const uint16_t* st = stage_tab(buf);
+    const uint32_t* se = stage_ev(buf);
+    const uint32_t* st = stage_tab(buf);
     const float2* sp = stage_pq(buf);
     float2 cache[E][RS][SW];
     int base[E][RS];
@@ -248,30 +251,29 @@ __device__ __forceinline__ void rows_chunk(
     // ---- forward: this warp's rows of every event of the batch
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      const bool valid = b * E + j < c.count;
-      const short4 box = sb[j];
-      const uint16_t* tab = st + j * stride;
+      // packed event word (row_coeff_kernel): window row of the box top,
+      // box rows, fits-the-shape flag; zero past the chunk's end
+      const uint32_t epk = se[j];
+      const uint32_t* tab = st + j * stride;
       const float2* pqt = sp + j * stride;
-      const int nrows = valid ? box.w - box.y : 0;
-      const int maxw = tab[stride - 1];
-      const bool fits = valid && nrows <= kPass * RS && maxw + 1 <= kSweep * SW;
+      const bool fits = (epk >> 31) != 0;
       fits_mask |= fits ? (1u << j) : 0u;
-      const int r0 = valid ? box.y - c.oy : 0;
-      const int col0 = valid ? box.x - ox : 0;
+      const int r0 = static_cast<int>(epk & 0xFFFu);
+      const int nrows = static_cast<int>((epk >> 12) & 0xFFFu);
       float2 den_a = make_float2(0.0f, 0.0f);
 #pragma unroll
       for (int rs = 0; rs < RS; ++rs) {
         const int ri = ((kRowsPerWarp * warp + gid - r0) & (kPass - 1)) + kPass * rs;
         const bool rv = fits && ri < nrows;
         const int ric = rv ? ri : 0;
+        // packed row word: window offset of the row's even start column (with
+        // the interval's parity in bit 0) and the interval width
         const uint32_t en = tab[ric];
         const float2 pqv = pqt[ric];
-        const int w = rv ? static_cast<int>(en >> 8) : 0;
-        const int lo = col0 + static_cast<int>(en & 255u);
-        const int a_off = lo & ~1;
-        const int lead = lo & 1;  // 0 or 1 pixels before the interval
+        const int w = rv ? static_cast<int>(en >> 24) : 0;
+        const int lead = static_cast<int>(en & 1u);  // 0 or 1 pixels before the interval
         const int end = lead + w;
-        const int bse = (r0 + ric) * pitch + a_off + 2 * gl;
+        const int bse = static_cast<int>(en & 0xFFFFFEu) + 2 * gl;
         base[j][rs] = bse;
         const float2 p2 = make_float2(pqv.x, pqv.x), q2 = make_float2(pqv.y, pqv.y);
 #pragma unroll
@@ -433,11 +435,11 @@ template <int NW, int G, int RS, int SW, int E, int ACC, bool DEN64>
 __global__ void __launch_bounds__(NW * 32, (NW == 8 ? 2 : 4)) iterate_rows_kernel(
     DevGeom g, FastConst fc, Tiling t, const Chunk* __restrict__ chunks,
     const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
-    const uint16_t* __restrict__ rows, const float2* __restrict__ row_pq,
-    const float* __restrict__ rho, float* __restrict__ out, double* __restrict__ out64,
-    DevCounters* counters, uint32_t seed) {
-  rows_chunk<NW, G, RS, SW, E, ACC, DEN64>(g, fc, t, chunks[blockIdx.x], ev_geom, ev_box, rows,
-                                           row_pq, rho, out, out64, counters, seed);
+    const uint32_t* __restrict__ ev_pk, const uint32_t* __restrict__ rows,
+    const float2* __restrict__ row_pq, const float* __restrict__ rho, float* __restrict__ out,
+    double* __restrict__ out64, DevCounters* counters, uint32_t seed) {
+  rows_chunk<NW, G, RS, SW, E, ACC, DEN64>(g, fc, t, chunks[blockIdx.x], ev_geom, ev_box, ev_pk,
+                                           rows, row_pq, rho, out, out64, counters, seed);
 }
 
 // Shapes name the rows an event may span (kPass * RS): the warps per CTA set
@@ -446,7 +448,8 @@ template <int NW, int G, int ROWS, int SW, int ACC, bool DEN64>
 cudaError_t launch_rows_kernel(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                const Chunk* chunks,
                                int32_t n_chunks, const float4* ev_geom, const short4* ev_box,
-                               const uint16_t* rows, const float2* pq, const float* rho,
+                               const uint32_t* ev_pk, const uint32_t* rows, const float2* pq,
+                               const float* rho,
                                float* out, double* out64, DevCounters* counters, uint32_t seed,
                                cudaStream_t s) {
   constexpr int kPass = NW * (32 / G);
@@ -458,33 +461,34 @@ cudaError_t launch_rows_kernel(const DevGeom& g, const FastConst& fc, const Tili
   cudaError_t err =
       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (err != cudaSuccess) return err;
-  k<<<n_chunks, NW * 32, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, rows, pq, rho, out, out64,
-                                    counters, seed);
+  k<<<n_chunks, NW * 32, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out,
+                                    out64, counters, seed);
   return cudaGetLastError();
 }
 
 template <int NW, int G, int ROWS, int SW>
 cudaError_t launch_rows_prec(const DevGeom& g, const FastConst& fc, const Tiling& t,
                              const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
-                             const short4* ev_box, const uint16_t* rows, const float2* pq,
+                             const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
+                              const float2* pq,
                              const float* rho, float* out, double* out64, DevCounters* counters,
                              int precision, uint32_t seed, cudaStream_t s) {
   switch (precision) {
     case kPrecisionCompensated:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccCompensated, false>(
-          g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho, out, out64, counters, seed,
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
           s);
     case kPrecisionCompensatedDen64:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccCompensated, true>(
-          g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho, out, out64, counters, seed,
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
           s);
     case kPrecisionFixed:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccFixed, false>(
-          g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho, out, out64, counters, seed,
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
           s);
     default:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccFloat, false>(
-          g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho, out, out64, counters, seed,
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
           s);
   }
 }
@@ -494,13 +498,14 @@ cudaError_t launch_rows_prec(const DevGeom& g, const FastConst& fc, const Tiling
 template <int G, int ROWS, int SW>
 cudaError_t launch_rows_shape(const DevGeom& g, const FastConst& fc, const Tiling& t,
                               const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
-                              const short4* ev_box, const uint16_t* rows, const float2* pq,
+                              const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
+                              const float2* pq,
                               const float* rho, float* out, double* out64, DevCounters* counters,
                               int precision, uint32_t seed, cudaStream_t s) {
   if (t.threads == 256)
-    return launch_rows_prec<8, G, ROWS, SW>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq,
+    return launch_rows_prec<8, G, ROWS, SW>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq,
                                             rho, out, out64, counters, precision, seed, s);
-  return launch_rows_prec<4, G, ROWS, SW>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq,
+  return launch_rows_prec<4, G, ROWS, SW>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq,
                                           rho, out, out64, counters, precision, seed, s);
 }
 
@@ -523,7 +528,7 @@ __global__ void __launch_bounds__(NW * 32, (NW == 8 ? 2 : 4))
     const BatchItem w = items[it];
     const BatchInstance& in = insts[w.inst];
     rows_chunk<NW, G, RS, SW, E, kAccFloat, false>(
-        in.g, in.fc, in.t, in.chunks[w.index], in.ev_geom, in.ev_box, in.rows, in.pq,
+        in.g, in.fc, in.t, in.chunks[w.index], in.ev_geom, in.ev_box, in.ev_pk, in.rows, in.pq,
         in.img[parity], in.img[parity ^ 1], nullptr, in.counters, 0u);
     __syncthreads();
   }
@@ -612,6 +617,15 @@ __global__ void batch_oversize_kernel(const BatchInstance* __restrict__ insts,
 
 }  // namespace
 
+int rows_shape_rows(int rows_shape) {
+  static const int rows[] = {32, 32, 64, 64, 64, 128, 64};
+  return (rows_shape >= 0 && rows_shape <= kRowsShape2x1x6) ? rows[rows_shape] : 128;
+}
+int rows_sweep_cols(int rows_shape) {
+  static const int cols[] = {16, 32, 16, 24, 32, 32, 24};
+  return (rows_shape >= 0 && rows_shape <= kRowsShape2x1x6) ? cols[rows_shape] : 32;
+}
+
 int rows_shape_for(int rows999, int width) {
   if (rows999 <= 32 && width <= 15) return kRowsShape8x1x1;
   if (rows999 <= 32 && width <= 31) return kRowsShape8x1x2;
@@ -623,7 +637,8 @@ int rows_shape_for(int rows999, int width) {
 
 cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
-                                const short4* ev_box, const uint16_t* rows, const float2* pq,
+                                const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
+                              const float2* pq,
                                 const float* rho, float* out, double* out64,
                                 DevCounters* counters, int precision, uint32_t seed,
                                 cudaStream_t s) {
@@ -631,25 +646,25 @@ cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Til
   if (t.chunk_events > kMaxChunkEvents || (t.row_stride & 7) != 0) return cudaErrorInvalidValue;
   switch (t.rows_shape) {
     case kRowsShape8x1x1:
-      return launch_rows_shape<8, 32, 1>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho,
+      return launch_rows_shape<8, 32, 1>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
                                          out, out64, counters, precision, seed, s);
     case kRowsShape8x1x2:
-      return launch_rows_shape<8, 32, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho,
+      return launch_rows_shape<8, 32, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
                                          out, out64, counters, precision, seed, s);
     case kRowsShape4x1x2:
-      return launch_rows_shape<4, 64, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho,
+      return launch_rows_shape<4, 64, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
                                          out, out64, counters, precision, seed, s);
     case kRowsShape4x1x3:
-      return launch_rows_shape<4, 64, 3>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho,
+      return launch_rows_shape<4, 64, 3>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
                                          out, out64, counters, precision, seed, s);
     case kRowsShape4x1x4:
-      return launch_rows_shape<4, 64, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho,
+      return launch_rows_shape<4, 64, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
                                          out, out64, counters, precision, seed, s);
     case kRowsShape2x1x6:
-      return launch_rows_shape<2, 64, 6>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho,
+      return launch_rows_shape<2, 64, 6>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
                                          out, out64, counters, precision, seed, s);
     default:
-      return launch_rows_shape<4, 128, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, pq, rho,
+      return launch_rows_shape<4, 128, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
                                           out, out64, counters, precision, seed, s);
   }
 }
