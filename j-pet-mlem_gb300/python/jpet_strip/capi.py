@@ -209,9 +209,11 @@ class Geometry:
     pixel: float
     sigma_z: float
     sigma_dl: float
+    pixel_height: float | None = None  # rows' height when it differs from the width
 
     def c(self) -> Geom:
-        return Geom(self.radius, self.length, self.n_y, self.n_z, self.pixel, self.pixel,
+        ph = self.pixel if self.pixel_height is None else self.pixel_height
+        return Geom(self.radius, self.length, self.n_y, self.n_z, ph, self.pixel,
                     self.sigma_z, self.sigma_dl)
 
 

@@ -48,10 +48,12 @@ class Geometry:
     pixel: float
     sigma_z: float
     sigma_dl: float
+    pixel_height: float | None = None  # rows' height when it differs from the width
 
     def c(self) -> OrcGeom:
-        return OrcGeom(self.radius, self.length, self.n_y, self.n_z, self.pixel,
-                       self.pixel, self.sigma_z, self.sigma_dl)
+        ph = self.pixel if self.pixel_height is None else self.pixel_height
+        return OrcGeom(self.radius, self.length, self.n_y, self.n_z, ph, self.pixel,
+                       self.sigma_z, self.sigma_dl)
 
 
 def build() -> str:

@@ -342,3 +342,29 @@ def test_fp64_reference_iteration_matches_fp64_oracle(golden):
     got2, _ = capi.reference_fp64(cg2, ev2, 2)
     want2 = O.mlem_d(og2, ev2, 2, threads=4)
     assert rel_l2(got2, want2) < 1e-12
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("grid", [(12, 16, 5.0, 5.0), (90, 120, 2.0, 3.0), (300, 200, 4.0, 2.5),
+                                  (7, 500, 2.0, 2.0)])
+def test_small_and_non_square_grids(grid, variant):
+    """Tiny grids (windows narrower than the widest sweep), rows taller or
+    shorter than the columns are wide, and a grid a few rows high: every kernel
+    against the oracle (the reference's Scanner keeps pixel_width and
+    pixel_height apart, scanner.h:39-67)."""
+    n_y, n_z, pw, ph = grid
+    ell = phantom.random_ellipse_phantom(seed=9, half_z=min(500.0, n_z * pw / 2),
+                                         half_y=min(450.0, n_y * ph / 2), centre_z=20.0,
+                                         centre_y=10.0, axes=(5.0, 200.0))
+    ev = phantom.generate_events(ell, 5000, 450.0, 1000.0, 10.0, 42.0, seed=9)
+    args = (450.0, 1000.0, n_y, n_z, pw, 10.0, 42.0)
+    cg = capi.Geometry(*args, pixel_height=ph)
+    og = O.Geometry(*args, pixel_height=ph)
+    want, st = O.mlem_f(og, ev, 2, threads=8)
+    with capi.StripReconstruction(cg, variant=variant) as rec:
+        rec.set_events(ev)
+        rec.iterate(2)
+        got = rec.rho
+        cnt = rec.counters()
+    assert rel_l2(got, want) < TOL_ITER
+    assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
