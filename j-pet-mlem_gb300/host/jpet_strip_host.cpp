@@ -281,6 +281,7 @@ Reconstruction<F>::Reconstruction(const Scanner& s, RunOptions o)
   opts.device = o.device;
   opts.mode = o.mode;
   opts.variant = o.variant;
+  opts.precision = o.precision;
   check(jpet_strip_create(&g, &opts, &handle_), nullptr, "jpet_strip_create");
   // point sensitivity at pixel centres (reconstruction.h:67-73)
   check(jpet_strip_get_sensitivity(handle_, 0, sensitivity.data), handle_, "sensitivity");

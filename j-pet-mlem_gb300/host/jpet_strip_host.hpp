@@ -120,6 +120,7 @@ struct RunOptions {
   int device = 0;
   int mode = JPET_MODE_CPU_REFERENCE;
   int variant = JPET_VARIANT_FAST;
+  int precision = JPET_PRECISION_FP32;
 };
 
 // Reconstruction<F, GaussianKernel<F>> with the reference's members

@@ -62,7 +62,13 @@ void add_options(Parser& cl) {
   cl.add("cuda-threads", 'W', "CUDA threads per block", Kind::Int, cmd::kDontSave, "512");
   cl.add("rho", 0, "start rho (eg. existing iteration)", Kind::Path, cmd::kOptional, "");
   cl.add_flag("rho-is-int", 0, "start rho uses integer representation (not float)");
-  cl.add("kernel", 0, "GPU kernel variant: 0 fast, 1 exact (reference operation order)",
+  cl.add("kernel", 0,
+         "GPU kernel variant: 0 fast (row-owned), 1 exact (reference operation order), "
+         "2 warp per event",
+         Kind::Int, cmd::kDontSave, "0");
+  cl.add("precision", 0,
+         "accumulation: 0 float, 1 compensated tiles, 2 compensated + FP64 denominators, "
+         "3 fixed-point tiles",
          Kind::Int, cmd::kDontSave, "0");
 }
 
@@ -179,6 +185,7 @@ int run(int argc, char* argv[]) {
   ro.device = cl.get_int("cuda-device");
   ro.mode = gpu_semantics ? JPET_MODE_GPU_REFERENCE : JPET_MODE_CPU_REFERENCE;
   ro.variant = cl.get_int("kernel");
+  ro.precision = cl.get_int("precision");
   Reconstruction reconstruction(scanner, ro);
 
   const int verbose = cl.count("verbose");

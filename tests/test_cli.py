@@ -38,12 +38,13 @@ def test_missing_input_and_bad_option():
 
 
 @pytest.mark.gpu
-def test_binary_input_matches_reference_golden(tmp_path, golden):
+@pytest.mark.parametrize("extra", [[], ["--precision", "1"], ["--kernel", "2"]])
+def test_binary_input_matches_reference_golden(tmp_path, golden, extra):
     manifest, load = golden
     ev = load("c1_events.npy")
     ev.tofile(tmp_path / "ev.bin")
     r = run([str(tmp_path / "ev.bin")] + GEOM + ["-i", "3", "-I", "1", "-o",
-                                                 str(tmp_path / "r.bin")])
+                                                 str(tmp_path / "r.bin")] + extra)
     assert r.returncode == 0, r.stderr
     for it in (1, 3):
         got = np.fromfile(tmp_path / f"r_{it}.bin", np.float32).reshape(180, 200)
