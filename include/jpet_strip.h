@@ -318,6 +318,11 @@ typedef struct jpet_strip_region {
  * (origin_x, origin_y) (--image-origin); row 0 is the lowest y.  emitted:
  * emission points of every emission counted; detected: emission points of the
  * detected events; naive: the points recovered from the smeared responses.
+ * tan_map (--tan-bins, phantom_cmd.cpp:243-253,339-345): int32[tan_bins * n_y *
+ * n_z], index (plane * n_y + row) * n_z + column, the naive points binned also
+ * by their tangent into tan_bins planes over +-1.1 L / 2R.  The naive and tan
+ * bins follow the reference's float arithmetic (response.h:22-37,
+ * pixel_grid.h:59-64, voxel_grid.h:109-118).
  * Device pointers for jpet_strip_generate, host pointers for
  * jpet_strip_generate_host; the device images are accumulated into, the host
  * ones overwritten. */
@@ -326,6 +331,9 @@ typedef struct jpet_strip_gen_images {
   int32_t* detected;
   int32_t* naive;
   double origin_x, origin_y;
+  int32_t tan_bins; /* planes of tan_map (0 = no map) */
+  int32_t reserved;
+  int32_t* tan_map;
 } jpet_strip_gen_images;
 
 /* Writes the detected, smeared responses (z_u, z_d, dl) as float triples to
@@ -348,6 +356,19 @@ int jpet_strip_generate_host(const jpet_strip_geom* geom, const jpet_strip_regio
                              int32_t n_regions, int64_t n, uint64_t seed, int32_t flags,
                              float* out_aos, int64_t capacity, int64_t* n_written,
                              const jpet_strip_gen_images* images, int32_t device);
+
+/* Kernel map of the phantom tool's --tan-bins output (phantom_cmd.cpp:396-436):
+ * float[tan_bins * n_y * n_z] into host memory `out`, index (plane * n_y + row)
+ * * n_z + column, the analytic kernel (analytic_kernel.h:28-74) of an event at
+ * each voxel centre (z, y, tangent of the plane) evaluated at the emission
+ * point (kernel_x, kernel_y) (--kernel-point), times 4 R pixel^2 dtan sec and,
+ * when divide_by_sensitivity (the reference's --detected), divided by the
+ * scanner sensitivity at the kernel point.  Grid and tangent planes as for
+ * jpet_strip_gen_images; geom supplies the scanner, the grid and the sigmas.
+ * Runs on device `device` and is complete on return. */
+int jpet_strip_tan_kernel_map(const jpet_strip_geom* geom, int32_t tan_bins, double kernel_x,
+                              double kernel_y, double origin_x, double origin_y,
+                              int32_t divide_by_sensitivity, float* out, int32_t device);
 
 #ifdef __cplusplus
 }

@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "../../include/jpet_strip.h"
+#include "strip_device.cuh"
 #include "strip_internal.h"
 
 namespace jpet {
@@ -102,9 +103,35 @@ struct GenImages {
   int32_t* emitted;   // emission points of all emissions counted
   int32_t* detected;  // emission points of the detected events
   int32_t* naive;     // points recovered from the smeared responses
+  int32_t* tan_map;   // the same, binned also by tangent
   double x0, y0, s;
-  int32_t n_z, n_y;
+  int32_t n_z, n_y, tan_bins;
+  // the grid in the reference's float: lower-left corner, pixel size, 2R, the
+  // first tangent plane's lower edge and the plane width
+  float fx0, fy0, fs, two_r, tan_left, tan_size;
 };
+
+// Naive point of a smeared response and its bins, in float without
+// contraction as the reference's host code computes them:
+// Response::calculate_tan_y_z (response.h:22-37), PixelGrid::pixel_at
+// (pixel_grid.h:59-64), VariableVoxelSizeVoxelGrid::voxel_at (voxel_grid.h:109-118).
+__device__ __forceinline__ void naive_add(const GenImages& im, float zu, float zd, float dl) {
+  const float t = __fdiv_rn(__fsub_rn(zu, zd), im.two_r);
+  const float y = __fmul_rn(-0.5f, __fdiv_rn(dl, __fsqrt_rn(__fadd_rn(1.0f, __fmul_rn(t, t)))));
+  const float z = __fmul_rn(0.5f, __fadd_rn(__fadd_rn(zu, zd), __fmul_rn(__fmul_rn(2.0f, y), t)));
+  const float col = floorf(__fdiv_rn(__fsub_rn(z, im.fx0), im.fs));
+  const float row = floorf(__fdiv_rn(__fsub_rn(y, im.fy0), im.fs));
+  if (!(col >= 0.0f && col < static_cast<float>(im.n_z) && row >= 0.0f &&
+        row < static_cast<float>(im.n_y)))
+    return;
+  const int pix = static_cast<int>(row) * im.n_z + static_cast<int>(col);
+  if (im.naive) atomicAdd(&im.naive[pix], 1);
+  if (im.tan_map) {
+    const float plane = floorf(__fdiv_rn(__fsub_rn(t, im.tan_left), im.tan_size));
+    if (plane >= 0.0f && plane < static_cast<float>(im.tan_bins))
+      atomicAdd(&im.tan_map[static_cast<size_t>(plane) * im.n_y * im.n_z + pix], 1);
+  }
+}
 
 __device__ __forceinline__ void image_add(int32_t* img, const GenImages& im, double z, double y) {
   if (!img) return;
@@ -237,13 +264,7 @@ __global__ void __launch_bounds__(kGenThreads) gen_kernel(
         image_add(im.emitted, im, c.px, c.py);
         if (take) {
           image_add(im.detected, im, c.px, c.py);
-          if (im.naive) {
-            // the reference's calculate_tan_y_z in float (response.h:13-37)
-            const float t = (c.zu - c.zd) / (2.0f * static_cast<float>(p.R));
-            const float y = -0.5f * c.dl / sqrtf(1.0f + t * t);
-            const float z = 0.5f * (c.zu + c.zd + 2.0f * y * t);
-            image_add(im.naive, im, z, y);
-          }
+          if (im.naive || im.tan_map) naive_add(im, c.zu, c.zd, c.dl);
         }
       }
       const unsigned m = __ballot_sync(0xffffffffu, take);
@@ -284,6 +305,59 @@ constexpr double kPi = 3.14159265358979323846;
 }  // namespace jpet
 
 using namespace jpet;
+
+// The phantom tool's float grids (phantom_cmd.cpp:241-253): PixelGrid with its
+// lower-left corner at float(-s n / 2) + float(origin), and the tangent planes
+// of VariableVoxelSizeVoxelGrid(-max_tan, bins, max_tan / bins * 2) with
+// max_tan = 1.1 L / 2R.
+namespace jpet {
+namespace {
+struct TanGrid {
+  float x0, y0, s, tan_left, tan_size;
+};
+TanGrid tan_grid(const jpet_strip_geom& g, int bins, double origin_x, double origin_y) {
+  TanGrid t;
+  t.s = static_cast<float>(g.pixel_width);
+  t.x0 = static_cast<float>(-g.pixel_width * g.n_z_pixels / 2) + static_cast<float>(origin_x);
+  t.y0 = static_cast<float>(-g.pixel_width * g.n_y_pixels / 2) + static_cast<float>(origin_y);
+  const float max_tan = 1.1f * static_cast<float>(g.scintillator_length) /
+                        (2.0f * static_cast<float>(g.radius));
+  t.tan_left = -max_tan;
+  t.tan_size = bins > 0 ? max_tan / static_cast<float>(bins) * 2.0f : 0.0f;
+  return t;
+}
+
+// One thread per voxel of the kernel map (phantom_cmd.cpp:402-430) in the
+// reference's float order: tangent of the plane centre, sec, the voxel centre,
+// AnalyticKernel at the kernel point, times the volume element 4 R bin_volume
+// sec and the inverse sensitivity.
+__global__ void __launch_bounds__(256) tan_kernel_map_kernel(DevGeom g, int32_t n_z, int32_t n_y,
+                                                             int32_t bins, TanGrid tg, float kx,
+                                                             float ky, float vol4r, float inv_sens,
+                                                             float* __restrict__ out) {
+  const size_t n = static_cast<size_t>(n_z) * n_y * bins;
+  const float llcx = __fadd_rn(tg.x0, __fmul_rn(tg.s, 0.5f));
+  const float llcy = __fadd_rn(tg.y0, __fmul_rn(tg.s, 0.5f));
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const int x = static_cast<int>(i % n_z);
+    const int y = static_cast<int>((i / n_z) % n_y);
+    const int z = static_cast<int>(i / (static_cast<size_t>(n_z) * n_y));
+    const float tan = __fadd_rn(__fmul_rn(__fadd_rn(static_cast<float>(z), 0.5f), tg.tan_size),
+                                tg.tan_left);
+    const float sec = __fsqrt_rn(__fadd_rn(1.0f, __fmul_rn(tan, tan)));
+    const float cx = __fadd_rn(llcx, __fmul_rn(static_cast<float>(x), tg.s));
+    const float cy = __fadd_rn(llcy, __fmul_rn(static_cast<float>(y), tg.s));
+    const float k = analytic_exact(g, cy, tan, sec, __fsub_rn(kx, cx), __fsub_rn(ky, cy));
+    out[i] = __fmul_rn(__fmul_rn(k, __fmul_rn(vol4r, sec)), inv_sens);
+  }
+}
+
+__global__ void sensitivity_at_kernel(DevGeom g, float px, float py, float* out) {
+  *out = scanner_sensitivity(g, px, py);
+}
+}  // namespace
+}  // namespace jpet
 
 extern "C" {
 
@@ -360,7 +434,11 @@ int jpet_strip_generate(const jpet_strip_geom* geom, const jpet_strip_region* re
   if (n == 0) return JPET_OK;
 
   GenImages im{};
-  if (images && (images->emitted || images->detected || images->naive)) {
+  if (images && (images->tan_bins < 0 || (images->tan_bins > 0) != (images->tan_map != nullptr))) {
+    set_call_error("jpet_strip_generate: tan_map needs tan_bins > 0 and the reverse");
+    return JPET_ERR_ARGUMENT;
+  }
+  if (images && (images->emitted || images->detected || images->naive || images->tan_map)) {
     if (geom->n_z_pixels <= 0 || geom->n_y_pixels <= 0 || !(geom->pixel_width > 0)) {
       set_call_error("jpet_strip_generate: count images need n_z, n_y and the pixel size");
       return JPET_ERR_ARGUMENT;
@@ -368,11 +446,20 @@ int jpet_strip_generate(const jpet_strip_geom* geom, const jpet_strip_region* re
     im.emitted = images->emitted;
     im.detected = images->detected;
     im.naive = images->naive;
+    im.tan_map = images->tan_map;
+    im.tan_bins = images->tan_bins;
     im.s = geom->pixel_width;
     im.n_z = geom->n_z_pixels;
     im.n_y = geom->n_y_pixels;
     im.x0 = -im.s * im.n_z / 2.0 + images->origin_x;
     im.y0 = -im.s * im.n_y / 2.0 + images->origin_y;
+    const TanGrid tg = tan_grid(*geom, im.tan_bins, images->origin_x, images->origin_y);
+    im.fx0 = tg.x0;
+    im.fy0 = tg.y0;
+    im.fs = tg.s;
+    im.two_r = 2.0f * static_cast<float>(geom->radius);
+    im.tan_left = tg.tan_left;
+    im.tan_size = tg.tan_size;
   }
   GenParams p;
   p.R = geom->radius;
@@ -483,20 +570,22 @@ int jpet_strip_generate_host(const jpet_strip_geom* geom, const jpet_strip_regio
   }
   const int64_t cap = std::max<int64_t>(std::min(capacity, n), 1);
   float* d_out = nullptr;
-  int32_t* d_img[3] = {nullptr, nullptr, nullptr};
-  int32_t* h_img[3] = {images ? images->emitted : nullptr, images ? images->detected : nullptr,
-                       images ? images->naive : nullptr};
+  int32_t* d_img[4] = {nullptr, nullptr, nullptr, nullptr};
+  int32_t* h_img[4] = {images ? images->emitted : nullptr, images ? images->detected : nullptr,
+                       images ? images->naive : nullptr, images ? images->tan_map : nullptr};
   const size_t n_pix = static_cast<size_t>(std::max(geom ? geom->n_y_pixels : 0, 0)) *
                        static_cast<size_t>(std::max(geom ? geom->n_z_pixels : 0, 0));
+  const size_t n_el[4] = {n_pix, n_pix, n_pix,
+                          n_pix * static_cast<size_t>(images ? std::max(images->tan_bins, 0) : 0)};
   auto release = [&]() {
     cudaFree(d_out);
     for (auto* q : d_img) cudaFree(q);
   };
   e = cudaMalloc(&d_out, static_cast<size_t>(cap) * 3 * sizeof(float));
-  for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+  for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
     if (!h_img[k]) continue;
-    e = cudaMalloc(&d_img[k], std::max<size_t>(n_pix, 1) * sizeof(int32_t));
-    if (e == cudaSuccess) e = cudaMemset(d_img[k], 0, n_pix * sizeof(int32_t));
+    e = cudaMalloc(&d_img[k], std::max<size_t>(n_el[k], 1) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemset(d_img[k], 0, n_el[k] * sizeof(int32_t));
   }
   if (e != cudaSuccess) {
     set_call_error(std::string("jpet_strip_generate_host: ") + cudaGetErrorString(e));
@@ -509,6 +598,7 @@ int jpet_strip_generate_host(const jpet_strip_geom* geom, const jpet_strip_regio
     dim.emitted = d_img[0];
     dim.detected = d_img[1];
     dim.naive = d_img[2];
+    dim.tan_map = d_img[3];
   }
   int64_t written = 0;
   int rc = jpet_strip_generate(geom, regions, n_regions, n, seed, flags, d_out, cap, &written,
@@ -516,8 +606,8 @@ int jpet_strip_generate_host(const jpet_strip_geom* geom, const jpet_strip_regio
   if (rc == JPET_OK) {
     e = cudaMemcpy(out_aos, d_out, static_cast<size_t>(written) * 3 * sizeof(float),
                    cudaMemcpyDeviceToHost);
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
-      if (h_img[k]) e = cudaMemcpy(h_img[k], d_img[k], n_pix * sizeof(int32_t),
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+      if (h_img[k]) e = cudaMemcpy(h_img[k], d_img[k], n_el[k] * sizeof(int32_t),
                                    cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {
       set_call_error(std::string("jpet_strip_generate_host: copy: ") + cudaGetErrorString(e));
@@ -527,6 +617,50 @@ int jpet_strip_generate_host(const jpet_strip_geom* geom, const jpet_strip_regio
   release();
   if (rc == JPET_OK && n_written) *n_written = written;
   return rc;
+}
+
+int jpet_strip_tan_kernel_map(const jpet_strip_geom* geom, int32_t tan_bins, double kernel_x,
+                              double kernel_y, double origin_x, double origin_y,
+                              int32_t divide_by_sensitivity, float* out, int32_t device) {
+  if (!geom || !out || tan_bins <= 0 || geom->n_z_pixels <= 0 || geom->n_y_pixels <= 0 ||
+      !(geom->pixel_width > 0) || !(geom->radius > 0) || !(geom->scintillator_length > 0) ||
+      !(geom->sigma_z > 0) || !(geom->sigma_dl > 0)) {
+    set_call_error("jpet_strip_tan_kernel_map: invalid argument");
+    return JPET_ERR_ARGUMENT;
+  }
+  const size_t n = static_cast<size_t>(geom->n_z_pixels) * geom->n_y_pixels * tan_bins;
+  cudaError_t e = cudaSetDevice(device);
+  float* d_out = nullptr;
+  float* d_sens = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&d_out, n * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&d_sens, sizeof(float));
+  const DevGeom g = make_dev_geom(*geom);
+  const TanGrid tg = tan_grid(*geom, tan_bins, origin_x, origin_y);
+  const float kx = static_cast<float>(kernel_x), ky = static_cast<float>(kernel_y);
+  float inv_sens = 1.0f;
+  if (e == cudaSuccess && divide_by_sensitivity) {
+    sensitivity_at_kernel<<<1, 1>>>(g, kx, ky, d_sens);
+    float sens = 0.0f;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(&sens, d_sens, sizeof(float), cudaMemcpyDeviceToHost);
+    inv_sens = 1.0f / sens;
+  }
+  // 4 R pixel^2 dtan (phantom_cmd.cpp:409-421), float left to right
+  const float vol4r = 4.0f * static_cast<float>(geom->radius) * (tg.s * tg.s * tg.tan_size);
+  if (e == cudaSuccess) {
+    const size_t blocks = std::min<size_t>((n + 255) / 256, 152 * 16);
+    tan_kernel_map_kernel<<<static_cast<unsigned>(blocks), 256>>>(
+        g, geom->n_z_pixels, geom->n_y_pixels, tan_bins, tg, kx, ky, vol4r, inv_sens, d_out);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d_out, n * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(d_out);
+  cudaFree(d_sens);
+  if (e != cudaSuccess) {
+    set_call_error(std::string("jpet_strip_tan_kernel_map: ") + cudaGetErrorString(e));
+    return JPET_ERR_CUDA;
+  }
+  return JPET_OK;
 }
 
 }  // extern "C"

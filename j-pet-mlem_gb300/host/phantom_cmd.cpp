@@ -7,11 +7,13 @@
 // Outputs: the smeared responses (z_u, z_d, dl) to --output, binary float
 // triples or, for a .txt name, one text line each; <base>.cfg with the options;
 // the int32 count images <base>_emitted, <base>_detected and <base>_naive with
-// their .nrrd headers.  The events follow a deterministic counter-based stream
-// selected by --seed (the reference seeds std::mt19937 per OpenMP thread, so
-// its output is not reproducible).  Not supported: --full, --no-responses,
-// --tan-bins, --kernel-point (the reference's extra diagnostic outputs) and
-// PNG previews.
+// their .nrrd headers; with --tan-bins also <base>_tan_bins (int32, the naive
+// points binned by tangent) and <base>_tan_kernel (float, the analytic kernel
+// of each voxel at --kernel-point), 3D maps of n_z x n_y x tan_bins.  The
+// events follow a deterministic counter-based stream selected by --seed (the
+// reference seeds std::mt19937 per OpenMP thread, so its output is not
+// reproducible).  Not supported: --full and --no-responses (the reference's
+// extra event dumps) and PNG previews.
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -121,15 +123,23 @@ void read_phantom(std::istream& in, double scale, std::vector<jpet_strip_region>
   }
 }
 
-void write_image(const std::string& base, const char* suffix, const std::vector<int32_t>& img,
-                 int n_z, int n_y) {
+const char* nrrd_type(const int32_t*) { return "int"; }
+const char* nrrd_type(const float*) { return "float"; }
+
+// raw map plus its NRRD header (nrrd_writer.h:18-27): 2D for depth 0, else 3D
+template <typename T>
+void write_image(const std::string& base, const char* suffix, const std::vector<T>& img, int n_z,
+                 int n_y, int depth = 0) {
   const std::string raw = base + suffix;
   std::ofstream o(raw, std::ios::binary);
-  o.write(reinterpret_cast<const char*>(img.data()), img.size() * sizeof(int32_t));
+  o.write(reinterpret_cast<const char*>(img.data()), img.size() * sizeof(T));
   if (!o) throw "cannot write " + raw;
   std::ofstream h(raw + ".nrrd");
-  h << "NRRD0001\ntype: int\nendian: little\ndimension: 2\nsizes: " << n_z << " " << n_y
-    << "\ndata file: ./" << raw << "\nencoding: raw\n";
+  h << "NRRD0001\ntype: " << nrrd_type(img.data())
+    << "\nendian: little\ndimension: " << (depth > 0 ? 3 : 2) << "\nsizes: " << n_z << " "
+    << n_y;
+  if (depth > 0) h << " " << depth;
+  h << "\ndata file: ./" << raw << "\nencoding: raw\n";
 }
 
 int run(int argc, char* argv[]) {
@@ -144,8 +154,17 @@ int run(int argc, char* argv[]) {
     }
     throw "at least one input phantom description expected, consult --help";
   }
-  for (const char* opt : {"full", "no-responses", "tan-bins", "kernel-point"})
+  for (const char* opt : {"full", "no-responses"})
     if (cl.exist(opt)) throw std::string("--") + opt + " is not supported by this tool";
+  const int tan_bins = cl.get_int("tan-bins");
+  if (tan_bins < 0) throw "--tan-bins must not be negative";
+  double kernel_x = 0, kernel_y = 0;
+  if (cl.exist("kernel-point")) {
+    auto kp = cl.get_doubles("kernel-point");
+    if (kp.size() != 2) throw "--kernel-point must supply exactly 2 values for x, y";
+    kernel_x = kp[0];
+    kernel_y = kp[1];
+  }
 
   const uint64_t n = cl.get_size("n-emissions");
   const int verbose = cl.count("verbose");
@@ -184,10 +203,15 @@ int run(int argc, char* argv[]) {
     im.origin_y = o[1];
   }
   const size_t n_pix = static_cast<size_t>(g.n_z_pixels) * static_cast<size_t>(g.n_y_pixels);
-  std::vector<int32_t> emitted(n_pix), det(n_pix), naive(n_pix);
+  std::vector<int32_t> emitted(n_pix), det(n_pix), naive(n_pix), tan_map;
   im.emitted = emitted.data();
   im.detected = det.data();
   im.naive = naive.data();
+  if (tan_bins > 0) {
+    tan_map.resize(n_pix * static_cast<size_t>(tan_bins));
+    im.tan_bins = tan_bins;
+    im.tan_map = tan_map.data();
+  }
   std::vector<float> ev(static_cast<size_t>(std::max<uint64_t>(n, 1)) * 3);
   int64_t written = 0;
   const int32_t flags = (cl.exist("detected") ? JPET_GEN_DETECTED : 0) |
@@ -228,6 +252,16 @@ int run(int argc, char* argv[]) {
   write_image(base, "_detected", det, g.n_z_pixels, g.n_y_pixels);
   write_image(base, "_emitted", emitted, g.n_z_pixels, g.n_y_pixels);
   write_image(base, "_naive", naive, g.n_z_pixels, g.n_y_pixels);
+  if (tan_bins > 0) {
+    write_image(base, "_tan_bins", tan_map, g.n_z_pixels, g.n_y_pixels, tan_bins);
+    if (verbose) std::cerr << "generating kernel map..." << std::endl;
+    std::vector<float> kmap(n_pix * static_cast<size_t>(tan_bins));
+    if (jpet_strip_tan_kernel_map(&g, tan_bins, kernel_x, kernel_y, im.origin_x, im.origin_y,
+                                  (flags & JPET_GEN_DETECTED) ? 1 : 0, kmap.data(),
+                                  cl.get_int("cuda-device")) != JPET_OK)
+      throw std::string(jpet_strip_last_error(nullptr));
+    write_image(base, "_tan_kernel", kmap, g.n_z_pixels, g.n_y_pixels, tan_bins);
+  }
   return 0;
 }
 

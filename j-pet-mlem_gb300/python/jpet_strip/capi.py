@@ -52,7 +52,7 @@ EXPORTED = [
     "jpet_strip_batch_last_error", "jpet_strip_batch_size", "jpet_strip_batch_instance",
     "jpet_strip_batch_set_events", "jpet_strip_batch_tune", "jpet_strip_batch_plan_of",
     "jpet_strip_batch_iterate", "jpet_strip_batch_launches_per_iteration",
-    "jpet_strip_reference_fp64",
+    "jpet_strip_reference_fp64", "jpet_strip_tan_kernel_map",
 ]
 
 
@@ -60,6 +60,19 @@ class StripError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"jpet_strip error {code}: {message}")
         self.code = code
+
+
+class GenImages(C.Structure):
+    _fields_ = [
+        ("emitted", C.c_void_p),
+        ("detected", C.c_void_p),
+        ("naive", C.c_void_p),
+        ("origin_x", C.c_double),
+        ("origin_y", C.c_double),
+        ("tan_bins", C.c_int32),
+        ("reserved", C.c_int32),
+        ("tan_map", C.c_void_p),
+    ]
 
 
 class Geom(C.Structure):
@@ -174,6 +187,9 @@ def lib() -> C.CDLL:
         L.jpet_strip_generate_host.argtypes = [C.POINTER(Geom), C.POINTER(Region), C.c_int32,
                                                C.c_int64, C.c_uint64, C.c_int32, vp, C.c_int64,
                                                C.POINTER(C.c_int64), vp, C.c_int32]
+        L.jpet_strip_tan_kernel_map.argtypes = [C.POINTER(Geom), C.c_int32, C.c_double,
+                                                C.c_double, C.c_double, C.c_double, C.c_int32,
+                                                vp, C.c_int32]
         L.jpet_strip_batch_create.argtypes = [C.c_int32, C.POINTER(Geom), C.POINTER(Opts),
                                               C.POINTER(vp)]
         L.jpet_strip_batch_destroy.argtypes = [vp]
@@ -276,6 +292,43 @@ def generate(regions, n: int, radius: float, length: float, sigma_z: float, sigm
     """As generate_device, copied to a host float32[k, 3] array."""
     return generate_device(regions, n, radius, length, sigma_z, sigma_dl, seed, detected,
                            additive, device).cpu().numpy()
+
+
+def generate_with_images(regions, n: int, geom: "Geometry", seed: int, detected: bool = True,
+                         additive: bool = False, origin=(0.0, 0.0), tan_bins: int = 0,
+                         device: int = 0):
+    """The phantom tool's outputs through jpet_strip_generate_host: the events
+    (float32[k, 3]) and the int32 count images on geom's grid (emitted,
+    detected, naive: [n_y, n_z], row 0 the lowest y; tan_map:
+    [tan_bins, n_y, n_z] when tan_bins > 0)."""
+    g = geom.c()
+    regs = _regions(regions)
+    shape = (geom.n_y, geom.n_z)
+    imgs = {k: np.zeros(shape, np.int32) for k in ("emitted", "detected", "naive")}
+    if tan_bins > 0:
+        imgs["tan_map"] = np.zeros((tan_bins,) + shape, np.int32)
+    im = GenImages(_ptr(imgs["emitted"]), _ptr(imgs["detected"]), _ptr(imgs["naive"]),
+                   float(origin[0]), float(origin[1]), int(tan_bins), 0,
+                   _ptr(imgs["tan_map"]) if tan_bins > 0 else None)
+    out = np.zeros((max(n, 1), 3), np.float32)
+    written = C.c_int64(0)
+    flags = (GEN_DETECTED if detected else 0) | (GEN_ADDITIVE if additive else 0)
+    _check(lib().jpet_strip_generate_host(C.byref(g), regs, len(regions), n, seed, flags,
+                                          _ptr(out), n, C.byref(written), C.byref(im), device))
+    return out[: written.value], imgs
+
+
+def tan_kernel_map(geom: "Geometry", tan_bins: int, kernel_point=(0.0, 0.0),
+                   origin=(0.0, 0.0), divide_by_sensitivity: bool = False,
+                   device: int = 0) -> np.ndarray:
+    """The phantom tool's --tan-bins kernel map, float32[tan_bins, n_y, n_z]."""
+    g = geom.c()
+    out = np.zeros((tan_bins, geom.n_y, geom.n_z), np.float32)
+    _check(lib().jpet_strip_tan_kernel_map(C.byref(g), tan_bins, float(kernel_point[0]),
+                                           float(kernel_point[1]), float(origin[0]),
+                                           float(origin[1]), int(bool(divide_by_sensitivity)),
+                                           _ptr(out), device))
+    return out
 
 
 def reference_fp64(geom: Geometry, events, n_iterations: int, rho=None, device: int = 0):

@@ -79,6 +79,10 @@ def lib():
         L.orc_mlem_d.argtypes = [gp, f32p, C.c_int64, f64p, C.c_int, C.c_int, C.POINTER(OrcStats)]
         L.orc_mlem_gpuref.argtypes = [gp, f32p, C.c_int64, f32p, C.c_int, C.c_int, C.c_void_p]
         L.orc_sensitivity_map_f.argtypes = [gp, C.c_int, f32p]
+        L.orc_naive_bins_f.argtypes = [gp, f32p, C.c_int64, C.c_double, C.c_double, C.c_int32,
+                                       C.c_void_p, C.c_void_p]
+        L.orc_tan_kernel_map_f.argtypes = [gp, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                           C.c_double, C.c_int32, f32p]
         L.orc_nll_grad.argtypes = [gp, C.c_double, C.c_double, f32p, C.c_int64, f32p,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                    C.POINTER(C.c_int64)]
@@ -193,6 +197,32 @@ def gaussian_kernel_d(sz, sdl, y, tan, sec, R, dz, dy) -> float:
 
 def analytic_kernel_d(sz, sdl, y, tan, sec, R, dz, dy) -> float:
     return lib().orc_analytic_kernel_d(sz, sdl, y, tan, sec, R, dz, dy)
+
+
+def naive_bins(geom: Geometry, events, origin=(0.0, 0.0), tan_bins: int = 0):
+    """The phantom tool's naive image int32[n_y, n_z] and, with tan_bins > 0,
+    its tangent-binned map int32[tan_bins, n_y, n_z] of smeared responses
+    (phantom_cmd.cpp:339-352; float, reference order)."""
+    ev = _events(events)
+    g = geom.c()
+    naive = np.zeros((geom.n_y, geom.n_z), np.int32)
+    tan = np.zeros((max(tan_bins, 1), geom.n_y, geom.n_z), np.int32)
+    lib().orc_naive_bins_f(C.byref(g), ev, len(ev),
+                           float(origin[0]), float(origin[1]), int(tan_bins),
+                           naive.ctypes.data, tan.ctypes.data if tan_bins > 0 else None)
+    return naive, (tan if tan_bins > 0 else None)
+
+
+def tan_kernel_map(geom: Geometry, tan_bins: int, kernel_point=(0.0, 0.0), origin=(0.0, 0.0),
+                   divide_by_sensitivity: bool = False) -> np.ndarray:
+    """The phantom tool's --tan-bins kernel map float32[tan_bins, n_y, n_z]
+    (phantom_cmd.cpp:396-430; float, reference order)."""
+    g = geom.c()
+    out = np.zeros((tan_bins, geom.n_y, geom.n_z), np.float32)
+    lib().orc_tan_kernel_map_f(C.byref(g), int(tan_bins), float(kernel_point[0]),
+                               float(kernel_point[1]), float(origin[0]), float(origin[1]),
+                               int(bool(divide_by_sensitivity)), out)
+    return out
 
 
 def event_box(geom: Geometry, z_u, z_d, dl):

@@ -166,6 +166,81 @@ void orc_sensitivity_map_f(const orc_geom* g, int kind, float* out) {
     }
 }
 
+/* The phantom tool's float grids (phantom_cmd.cpp:241-253): PixelGrid lower-left
+ * corner Point<F>(-s n_z / 2, -s n_y / 2) + origin, pixel size F(s); tangent
+ * planes of VariableVoxelSizeVoxelGrid(pixel_grid, -max_tan, bins,
+ * max_tan / bins * 2) with max_tan = (F)1.1 L / (2 R) (scanner fields float). */
+typedef struct {
+  float x0, y0, s, tan_left, tan_size;
+} tan_grid_f;
+
+static tan_grid_f tan_grid_init(const orc_geom* g, int bins, double ox, double oy) {
+  tan_grid_f t;
+  t.s = (float)g->pixel_width;
+  t.x0 = (float)(-g->pixel_width * g->n_z_pixels / 2) + (float)ox;
+  t.y0 = (float)(-g->pixel_width * g->n_y_pixels / 2) + (float)oy;
+  float max_tan = (float)1.1 * (float)g->scintillator_length / (2 * (float)g->radius);
+  t.tan_left = -max_tan;
+  t.tan_size = bins > 0 ? max_tan / bins * 2 : 0.0f;
+  return t;
+}
+
+/* Naive image and tangent-binned map of smeared responses (phantom_cmd.cpp:
+ * 339-352): from_projection_space_tan (scanner.h:122-127, response.h:22-37),
+ * PixelGrid::pixel_at (pixel_grid.h:59-64) and
+ * VariableVoxelSizeVoxelGrid::voxel_at (voxel_grid.h:109-118), all in float;
+ * voxel index (plane * n_y + row) * n_z + column (voxel.h:27-29).  naive and
+ * tan_map (bins > 0) may be NULL; both are accumulated into. */
+void orc_naive_bins_f(const orc_geom* g, const float* ev, int64_t n, double ox, double oy,
+                      int32_t bins, int32_t* naive, int32_t* tan_map) {
+  const tan_grid_f t = tan_grid_init(g, bins, ox, oy);
+  const float R = (float)g->radius;
+  const int nz = g->n_z_pixels, ny = g->n_y_pixels;
+  for (int64_t i = 0; i < n; ++i) {
+    float tan, y, z;
+    tan_y_z_f(R, ev[3 * i], ev[3 * i + 1], ev[3 * i + 2], &tan, &y, &z);
+    float fc = floorf((z - t.x0) / t.s), fr = floorf((y - t.y0) / t.s);
+    if (!(fc >= 0 && fc < nz && fr >= 0 && fr < ny)) continue;
+    int64_t pix = (int64_t)fr * nz + (int64_t)fc;
+    if (naive) naive[pix] += 1;
+    if (tan_map && bins > 0) {
+      float fp = floorf((tan - t.tan_left) / t.tan_size);
+      if (fp >= 0 && fp < bins) tan_map[(int64_t)fp * ny * nz + pix] += 1;
+    }
+  }
+}
+
+/* The --tan-bins kernel map (phantom_cmd.cpp:396-430), float: for every voxel
+ * the tangent of the plane centre (voxel_grid.h:105-107), sec, the pixel
+ * centre (pixel_grid.h:54-57), AnalyticKernel at the kernel point
+ * (analytic_kernel.h:65-74), the volume element 4 R pixel^2 dtan sqrt(1+tan^2)
+ * and the inverse sensitivity at the kernel point when divide (the
+ * reference's --detected). */
+void orc_tan_kernel_map_f(const orc_geom* g, int32_t bins, double kx_d, double ky_d, double ox,
+                          double oy, int32_t divide, float* out) {
+  const tan_grid_f t = tan_grid_init(g, bins, ox, oy);
+  orc_kernel_f k;
+  kernel_init_f((float)g->sigma_z, (float)g->sigma_dl, &k);
+  orc_scanner_f sc;
+  scanner_init_f(g, &sc);
+  const float kx = (float)kx_d, ky = (float)ky_d, R = (float)g->radius;
+  const float inv_sens = divide ? 1 / sens_f(&sc, kx, ky) : (float)1;
+  const float llcx = t.x0 + t.s / 2, llcy = t.y0 + t.s / 2;
+  const float bin_volume = t.s * t.s * t.tan_size;
+  const int nz = g->n_z_pixels, ny = g->n_y_pixels;
+  for (int z = 0; z < bins; ++z) {
+    float tan = ((int16_t)z + (float)0.5) * t.tan_size + t.tan_left;
+    float sec = sqrtf(1 + tan * tan);
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nz; ++x) {
+        float cx = llcx + (int16_t)x * t.s, cy = llcy + (int16_t)y * t.s;
+        float kv = analytic_f(&k, cy, tan, sec, R, kx - cx, ky - cy);
+        float volume_elem = 4 * R * bin_volume * sqrtf(1 + tan * tan);
+        out[((int64_t)z * ny + y) * nz + x] = kv * volume_elem * inv_sens;
+      }
+  }
+}
+
 int32_t orc_event_box_f(const orc_geom* g, float z_u, float z_d, float dl, int32_t* tl_x,
                         int32_t* tl_y, int32_t* br_x, int32_t* br_y) {
   orc_scanner_f s;

@@ -72,6 +72,13 @@ void orc_to_projection_space_tan_d(double R, double y, double z, double tan,
  * kind 0: point sensitivity at pixel centres (reconstruction.h:67-73).
  * kind 1: 5-point pixel sensitivity (scanner.h:174-185, cuda/reconstruction.cu:115-126). */
 void orc_sensitivity_map_f(const orc_geom* g, int kind, float* out);
+/* Naive image and tangent-binned map of smeared responses in the phantom
+ * tool's float arithmetic (phantom_cmd.cpp:241-253,339-352). */
+void orc_naive_bins_f(const orc_geom* g, const float* ev, int64_t n, double ox, double oy,
+                      int32_t bins, int32_t* naive, int32_t* tan_map);
+/* The phantom tool's --tan-bins kernel map (phantom_cmd.cpp:396-430). */
+void orc_tan_kernel_map_f(const orc_geom* g, int32_t bins, double kx, double ky, double ox,
+                          double oy, int32_t divide, float* out);
 
 /* Bounding box of one event after clamping (reconstruction.h:223-246);
  * returns in-ellipse pixel count; box = [tl_x, br_x) x [tl_y, br_y). */

@@ -128,3 +128,44 @@ def test_batch_create_rejects_unsupported_options_without_device():
     assert L.jpet_strip_batch_create(1, arr, C.byref(o), C.byref(b)) == capi.JPET_ERR_UNSUPPORTED
     assert L.jpet_strip_batch_create(0, arr, None, C.byref(b)) == capi.JPET_ERR_ARGUMENT
     assert L.jpet_strip_batch_destroy(None) == capi.JPET_OK
+
+
+def test_tan_map_and_kernel_map_argument_checks_need_no_device():
+    L = capi.lib()
+    g = capi.Geom(450.0, 1000.0, 18, 20, 5.0, 5.0, 10.0, 42.0)
+    regs = capi._regions([phantom_ellipse()])
+    n = C.c_int64(0)
+    out = (C.c_float * 30)()
+    # a map without planes, planes without a map
+    for bins, ptr in [(0, C.cast(out, C.c_void_p)), (4, None), (-1, None)]:
+        im = capi.GenImages(None, None, None, 0.0, 0.0, bins, 0, ptr)
+        assert L.jpet_strip_generate(C.byref(g), regs, 1, 10, 1, 1, C.cast(out, C.c_void_p), 10,
+                                     C.byref(n), C.byref(im), None) == capi.JPET_ERR_ARGUMENT
+        assert b"tan_map" in L.jpet_strip_last_error(None)
+    buf = (C.c_float * (18 * 20 * 2))()
+    assert L.jpet_strip_tan_kernel_map(C.byref(g), 0, 0.0, 0.0, 0.0, 0.0, 0, buf, 0) \
+        == capi.JPET_ERR_ARGUMENT
+    assert L.jpet_strip_tan_kernel_map(C.byref(g), 2, 0.0, 0.0, 0.0, 0.0, 0, None, 0) \
+        == capi.JPET_ERR_ARGUMENT
+    bad = capi.Geom(450.0, 1000.0, 18, 20, 5.0, 5.0, 0.0, 42.0)
+    assert L.jpet_strip_tan_kernel_map(C.byref(bad), 2, 0.0, 0.0, 0.0, 0.0, 0, buf, 0) \
+        == capi.JPET_ERR_ARGUMENT
+
+
+def test_oracle_tan_maps_are_consistent():
+    """The oracle's tangent map refines its naive image (planes sum to at most
+    the image), and its kernel map is finite, non-negative and peaks near the
+    kernel point."""
+    import numpy as np
+
+    import oracle as O
+
+    og = O.Geometry(450.0, 1000.0, 90, 100, 10.0, 10.0, 42.0)
+    ev = np.load(os.path.join(ROOT, "tests", "golden", "c1_events.npy"))[:20000]
+    naive, tan = O.naive_bins(og, ev, tan_bins=8)
+    assert naive.sum() > 0 and (tan.sum(0) <= naive).all() and tan.sum() > 0.9 * naive.sum()
+    m = O.tan_kernel_map(og, 8, (20.0, -10.0))
+    assert np.isfinite(m).all() and (m >= 0).all()
+    _, row, col = np.unravel_index(np.argmax(m), m.shape)
+    # grid row 0 is the lowest y: pixel centre -450 + 10 (row + 0.5)
+    assert abs(-500 + 10 * (col + 0.5) - 20.0) <= 10 and abs(-450 + 10 * (row + 0.5) + 10.0) <= 10

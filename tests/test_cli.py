@@ -113,6 +113,13 @@ def test_phantom_tool_usage_and_errors(tmp_path):
     r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "-e", "10", "--full",
                      str(tmp_path / "bad.txt")])
     assert r.returncode == 1 and "not supported" in r.stderr
+    golden = os.path.join(ROOT, "tests", "golden", "phantom_three.txt")
+    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "-e", "10", "--tan-bins", "-2",
+                     golden])
+    assert r.returncode == 1 and "--tan-bins must not be negative" in r.stderr
+    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "-e", "10", "--tan-bins", "4",
+                     "--kernel-point", "1,2,3", golden])
+    assert r.returncode == 1 and "--kernel-point must supply exactly 2 values" in r.stderr
 
 
 @pytest.mark.gpu
@@ -140,6 +147,20 @@ def test_phantom_then_reconstruction_tool_chain(tmp_path):
     assert r.returncode == 0, r.stderr
     ev2 = np.loadtxt(tmp_path / "ph2.txt", dtype=np.float32).reshape(-1, 3)
     assert ev2.shape == ev.shape and np.allclose(ev2, ev, rtol=1e-5, atol=1e-3)
+    # --tan-bins: the tangent-binned naive map and the kernel map (3D NRRD)
+    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "--n-z-pixels", "200",
+                     "--n-y-pixels", "180", "--s-z", "10", "--s-dl", "42", "-e", "200000",
+                     "--seed", "7", "--tan-bins", "6", "--kernel-point", "20,-10", "--detected",
+                     "-o", str(tmp_path / "pt.bin"), golden])
+    assert r.returncode == 0, r.stderr
+    tmap = np.fromfile(tmp_path / "pt_tan_bins", np.int32).reshape(6, 180, 200)
+    kmap = np.fromfile(tmp_path / "pt_tan_kernel", np.float32).reshape(6, 180, 200)
+    naive_t = np.fromfile(tmp_path / "pt_naive", np.int32).reshape(180, 200)
+    assert 0 < tmap.sum() <= naive_t.sum() and (tmap.sum(0) <= naive_t).all()
+    assert np.isfinite(kmap).all() and kmap.max() > 0
+    hdr = (tmp_path / "pt_tan_kernel.nrrd").read_text()
+    assert "type: float" in hdr and "dimension: 3" in hdr and "sizes: 200 180 6" in hdr
+    assert "type: int" in (tmp_path / "pt_tan_bins.nrrd").read_text()
     # reconstruction with the options of the accompanying .cfg only
     r = run([str(tmp_path / "ph.bin"), "-i", "2", "-I", "1", "-o", str(tmp_path / "r.bin")])
     assert r.returncode == 0, r.stderr

@@ -101,3 +101,50 @@ def test_point_and_rectangle_regions_and_additive_flag():
         frac.append((z * z + y * y < 50.0 ** 2).mean())
     # uniform density: the inner disc holds ~1/4 of the emissions; additive: 2/5
     assert 0.2 < frac[0] < 0.3 and 0.35 < frac[1] < 0.45, frac
+
+
+@pytest.mark.parametrize("detected", [True, False])
+def test_count_images_and_tan_map_match_the_oracle_binning(detected):
+    """Count images of the phantom tool: the naive image and the tangent-binned
+    map of the returned responses equal the oracle's float binning exactly
+    (shifted grid origin included); every detected emission point is also an
+    emitted one; emissions inside the grid are all counted."""
+    import oracle as O
+
+    ell = phantom.three_ellipse_phantom()
+    geom = capi.Geometry(R, L, 180, 200, 5.0, 10.0, 42.0)
+    og = O.Geometry(R, L, 180, 200, 5.0, 10.0, 42.0)
+    origin = (7.5, -3.0)
+    ev, im = capi.generate_with_images(ell, 300000, geom, seed=3, detected=detected,
+                                       origin=origin, tan_bins=12)
+    naive, tan = O.naive_bins(og, ev, origin=origin, tan_bins=12)
+    assert np.array_equal(im["naive"], naive)
+    assert np.array_equal(im["tan_map"], tan)
+    assert (im["emitted"] >= im["detected"]).all()
+    assert im["detected"].sum() == len(ev)  # the phantom lies inside the grid
+    if not detected:
+        assert im["emitted"].sum() == 300000
+    assert 0 < tan.sum() <= naive.sum() <= len(ev)
+    # the same events as without images
+    plain = capi.generate(ell, 300000, R, L, 10.0, 42.0, seed=3, detected=detected)
+    assert np.array_equal(plain, ev)
+
+
+@pytest.mark.parametrize("divide", [False, True])
+def test_tan_kernel_map_matches_the_oracle(divide):
+    """The --tan-bins kernel map against the oracle's float restatement of the
+    reference loop: the same float operations in the same order, with CUDA's
+    expf/atanf for the C library's (a few ulp)."""
+    import oracle as O
+
+    geom = capi.Geometry(R, L, 90, 100, 10.0, 10.0, 42.0)
+    og = O.Geometry(R, L, 90, 100, 10.0, 10.0, 42.0)
+    kp, origin = (20.0, -10.0), (5.0, 0.0)
+    got = capi.tan_kernel_map(geom, 16, kp, origin=origin, divide_by_sensitivity=divide)
+    want = O.tan_kernel_map(og, 16, kp, origin=origin, divide_by_sensitivity=divide)
+    assert got.shape == (16, 90, 100) and np.isfinite(got).all()
+    scale = float(want.max())
+    assert scale > 0
+    assert float(np.max(np.abs(got - want))) <= 2e-6 * scale
+    big = want > 1e-3 * scale
+    np.testing.assert_allclose(got[big], want[big], rtol=2e-6)
