@@ -70,7 +70,7 @@ struct jpet_strip {
 
   DevBuf<float> rho, out, sens_point, sens_pixel;
   DevBuf<double> out64;              // FP64 image of the compensated modes
-  DevBuf<float> raw;                 // staging for uploaded SoA events
+  DevBuf<float> raw;                 // staging for uploaded events (kept for the next upload)
   DevBuf<float4> ev_geom, sorted_geom, over_geom;
   DevBuf<short4> ev_box, sorted_box, over_box;
   DevBuf<int32_t> ev_key, tile_count, tile_offset, tile_cursor, hist, small;
@@ -254,7 +254,7 @@ int fast_width_shape(const DevGeom& g) {
 }
 
 int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const float* d_dl,
-                   int64_t n) {
+                   int64_t n, int32_t stride = 1) {
   cudaStream_t s = h->stream;
   h->events_ready = false;
   h->n_events = n;
@@ -273,7 +273,7 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
   JPET_CUDA(h, cudaMemsetAsync(h->hist.p, 0, 2 * kHistBins * sizeof(int32_t), s), "memset");
   JPET_CUDA(h, cudaMemsetAsync(h->box_pixels.p, 0, sizeof(unsigned long long), s), "memset");
   JPET_CUDA(h, cudaMemsetAsync(h->small.p, 0, 4 * sizeof(int32_t), s), "memset");
-  JPET_CUDA(h, launch_prep_events(h->g, d_zu, d_zd, d_dl, n, h->ev_geom.p, h->ev_box.p,
+  JPET_CUDA(h, launch_prep_events(h->g, d_zu, d_zd, d_dl, stride, n, h->ev_geom.p, h->ev_box.p,
                                   h->hist.p, h->hist.p + kHistBins, h->box_pixels.p, s),
             "prep_events launch");
   std::vector<int32_t> hist(2 * kHistBins);
@@ -398,23 +398,20 @@ int upload_and_prepare(jpet_strip* h, const float* zu, const float* zd, const fl
   float* d_dl = h->raw.p + 2 * n;
   cudaStream_t s = h->stream;
   if (aos) {
-    // AoS -> SoA with three strided 2D copies (the reference's ResponsesSOA
-    // transposed on the host, cuda/gpu_events_soa.h:15-44)
-    for (int c = 0; c < 3; ++c) {
-      JPET_CUDA(h, cudaMemcpy2DAsync(h->raw.p + c * n, sizeof(float), aos + c, 3 * sizeof(float),
-                                     sizeof(float), static_cast<size_t>(n),
-                                     cudaMemcpyHostToDevice, s),
-                "copy events");
-    }
+    // one contiguous copy of the AoS triples; the preparation kernel reads
+    // them with stride 3 (the reference transposes to SoA on the host,
+    // cuda/gpu_events_soa.h:15-44)
+    JPET_CUDA(h, cudaMemcpyAsync(h->raw.p, aos, 3 * static_cast<size_t>(n) * sizeof(float),
+                                 cudaMemcpyHostToDevice, s),
+              "copy events");
+    return prepare_events(h, h->raw.p, h->raw.p + 1, h->raw.p + 2, n, 3);
   } else {
     const size_t bytes = static_cast<size_t>(n) * sizeof(float);
     JPET_CUDA(h, cudaMemcpyAsync(d_zu, zu, bytes, cudaMemcpyHostToDevice, s), "copy z_u");
     JPET_CUDA(h, cudaMemcpyAsync(d_zd, zd, bytes, cudaMemcpyHostToDevice, s), "copy z_d");
     JPET_CUDA(h, cudaMemcpyAsync(d_dl, dl, bytes, cudaMemcpyHostToDevice, s), "copy dl");
   }
-  int rc = prepare_events(h, d_zu, d_zd, d_dl, n);
-  h->raw.release();
-  return rc;
+  return prepare_events(h, d_zu, d_zd, d_dl, n);
 }
 
 }  // namespace

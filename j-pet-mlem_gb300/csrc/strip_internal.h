@@ -94,9 +94,11 @@ void set_call_error(const std::string& msg);
 constexpr int kHistBins = 4096;  // box width/height histogram bins (last bin: >= 4095)
 
 // ---- launchers (strip_kernels.cu) -----------------------------------------------
+// z_u[i * stride], z_d[i * stride], dl[i * stride]: stride 1 for three arrays,
+// 3 for AoS triples (z_d = z_u + 1, dl = z_u + 2)
 cudaError_t launch_prep_events(const DevGeom& g, const float* z_u, const float* z_d,
-                               const float* dl, int64_t n, float4* ev_geom, short4* ev_box,
-                               int32_t* hist_w, int32_t* hist_h,
+                               const float* dl, int32_t stride, int64_t n, float4* ev_geom,
+                               short4* ev_box, int32_t* hist_w, int32_t* hist_h,
                                unsigned long long* box_pixels, cudaStream_t s);
 cudaError_t launch_key_events(const Tiling& t, int64_t n, const short4* ev_box, int32_t* ev_key,
                               int32_t* tile_count, int32_t* n_oversize, cudaStream_t s);

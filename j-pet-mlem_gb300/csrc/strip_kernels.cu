@@ -31,27 +31,44 @@ namespace {
 
 // Pass 1: per-event set-up (tan, y, z, sec and the clamped box) and histograms
 // of the box width and height, from which the host sizes the image windows.
-__global__ void prep_events_kernel(DevGeom g, const float* __restrict__ z_u,
-                                   const float* __restrict__ z_d,
-                                   const float* __restrict__ dl, int64_t n,
-                                   float4* __restrict__ ev_geom, short4* __restrict__ ev_box,
-                                   int32_t* hist_w, int32_t* hist_h,
-                                   unsigned long long* box_pixels) {
-  int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+// Events as three arrays (stride 1) or as AoS triples (z_u = base, z_d = base
+// + 1, dl = base + 2, stride 3).  The box-size histograms take one atomic per
+// distinct value in a warp (the events of a warp mostly share their box size)
+// and the box pixels one atomic per block.
+__global__ void __launch_bounds__(256) prep_events_kernel(
+    DevGeom g, const float* __restrict__ z_u, const float* __restrict__ z_d,
+    const float* __restrict__ dl, int32_t stride, int64_t n, float4* __restrict__ ev_geom,
+    short4* __restrict__ ev_box, int32_t* hist_w, int32_t* hist_h,
+    unsigned long long* box_pixels) {
+  __shared__ unsigned long long block_pixels[8];
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
   unsigned long long pixels = 0;
+  int kw = -1, kh = -1;
   if (i < n) {
-    EventSetup e = event_setup(g, z_u[i], z_d[i], dl[i]);
+    const int64_t j = i * stride;
+    EventSetup e = event_setup(g, z_u[j], z_d[j], dl[j]);
     ev_geom[i] = make_float4(e.z, e.y, e.tan, e.sec);
     ev_box[i] = make_short4(e.tl_x, e.tl_y, e.br_x, e.br_y);
     int bw = e.br_x - e.tl_x, bh = e.br_y - e.tl_y;
     if (bw > 0 && bh > 0) {
       pixels = static_cast<unsigned long long>(bw) * static_cast<unsigned long long>(bh);
-      atomicAdd(&hist_w[min(bw, kHistBins - 1)], 1);
-      atomicAdd(&hist_h[min(bh, kHistBins - 1)], 1);
+      kw = min(bw, kHistBins - 1);
+      kh = min(bh, kHistBins - 1);
     }
   }
+  const unsigned mw = __match_any_sync(0xffffffffu, kw);
+  if (kw >= 0 && lane == __ffs(mw) - 1) atomicAdd(&hist_w[kw], __popc(mw));
+  const unsigned mh = __match_any_sync(0xffffffffu, kh);
+  if (kh >= 0 && lane == __ffs(mh) - 1) atomicAdd(&hist_h[kh], __popc(mh));
   pixels = warp_sum_u64(pixels);
-  if ((threadIdx.x & 31) == 0 && pixels) atomicAdd(box_pixels, pixels);
+  if (lane == 0) block_pixels[threadIdx.x >> 5] = pixels;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tot = 0;
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) tot += block_pixels[w];
+    if (tot) atomicAdd(box_pixels, tot);
+  }
 }
 
 // Pass 2: tile key per event.  -1: empty box (the event contributes nothing,
@@ -191,14 +208,14 @@ __global__ void sensitivity_kernel(DevGeom g, int kind, float* __restrict__ out)
 // ---------------------------------------------------------------------------------
 
 cudaError_t launch_prep_events(const DevGeom& g, const float* z_u, const float* z_d,
-                               const float* dl, int64_t n, float4* ev_geom, short4* ev_box,
-                               int32_t* hist_w, int32_t* hist_h,
+                               const float* dl, int32_t stride, int64_t n, float4* ev_geom,
+                               short4* ev_box, int32_t* hist_w, int32_t* hist_h,
                                unsigned long long* box_pixels, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int threads = 256;
   const unsigned blocks = static_cast<unsigned>((n + threads - 1) / threads);
-  prep_events_kernel<<<blocks, threads, 0, s>>>(g, z_u, z_d, dl, n, ev_geom, ev_box, hist_w,
-                                                hist_h, box_pixels);
+  prep_events_kernel<<<blocks, threads, 0, s>>>(g, z_u, z_d, dl, stride, n, ev_geom, ev_box,
+                                                hist_w, hist_h, box_pixels);
   return cudaGetLastError();
 }
 
