@@ -12,8 +12,8 @@
 // of each voxel at --kernel-point), 3D maps of n_z x n_y x tan_bins.  The
 // events follow a deterministic counter-based stream selected by --seed (the
 // reference seeds std::mt19937 per OpenMP thread, so its output is not
-// reproducible).  Not supported: --full and --no-responses (the reference's
-// extra event dumps) and PNG previews.
+// reproducible).  --no-responses skips the responses file and keeps the rest.
+// Not supported: --full (the reference's extra event dumps) and PNG previews.
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -154,8 +154,7 @@ int run(int argc, char* argv[]) {
     }
     throw "at least one input phantom description expected, consult --help";
   }
-  for (const char* opt : {"full", "no-responses"})
-    if (cl.exist(opt)) throw std::string("--") + opt + " is not supported by this tool";
+  if (cl.exist("full")) throw std::string("--full is not supported by this tool");
   const int tan_bins = cl.get_int("tan-bins");
   if (tan_bins < 0) throw "--tan-bins must not be negative";
   double kernel_x = 0, kernel_y = 0;
@@ -235,7 +234,9 @@ int run(int argc, char* argv[]) {
 
   const std::string output = cl.get_path("output");
   const std::string base = cmd::path_wo_ext(output), ext = cmd::path_ext(output);
-  if (ext == ".txt") {
+  if (cl.exist("no-responses")) {
+    // the reference writes no responses file (phantom_cmd.cpp:210-232)
+  } else if (ext == ".txt") {
     std::ofstream o(output);
     for (int64_t i = 0; i < written; ++i)
       o << ev[3 * i] << ' ' << ev[3 * i + 1] << ' ' << ev[3 * i + 2] << '\n';

@@ -147,6 +147,13 @@ def test_phantom_then_reconstruction_tool_chain(tmp_path):
     assert r.returncode == 0, r.stderr
     ev2 = np.loadtxt(tmp_path / "ph2.txt", dtype=np.float32).reshape(-1, 3)
     assert ev2.shape == ev.shape and np.allclose(ev2, ev, rtol=1e-5, atol=1e-3)
+    # --no-responses: images and .cfg only
+    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "--n-z-pixels", "200",
+                     "--n-y-pixels", "180", "--s-z", "10", "--s-dl", "42", "-e", "20000",
+                     "--seed", "7", "--no-responses", "-o", str(tmp_path / "nr.bin"), golden])
+    assert r.returncode == 0, r.stderr
+    assert not (tmp_path / "nr.bin").exists() and (tmp_path / "nr_naive").exists()
+    assert (tmp_path / "nr.cfg").exists()
     # --tan-bins: the tangent-binned naive map and the kernel map (3D NRRD)
     r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "--n-z-pixels", "200",
                      "--n-y-pixels", "180", "--s-z", "10", "--s-dl", "42", "-e", "200000",

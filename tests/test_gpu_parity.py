@@ -368,3 +368,44 @@ def test_small_and_non_square_grids(grid, variant):
         cnt = rec.counters()
     assert rel_l2(got, want) < TOL_ITER
     assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
+
+
+def test_upload_paths_agree(golden):
+    """Host AoS (one contiguous copy read with stride 3), host SoA and device SoA
+    uploads prepare the same events: the same image and counters, repeated
+    uploads of different sizes included (the staging buffer is reused)."""
+    import ctypes as C
+
+    import torch
+
+    manifest, load = golden
+    cg, og = _geoms(manifest["c1"])
+    ev = load("c1_events.npy")
+    want, st = O.mlem_f(og, ev, 1, threads=4)
+    soa = np.ascontiguousarray(ev.T)
+    dev = torch.from_numpy(soa).to("cuda:0")
+    imgs, cnts = [], []
+    with capi.StripReconstruction(cg) as rec:
+        for how in ("aos_small", "aos", "soa", "device", "aos"):
+            if how == "aos_small":
+                rec.set_events(ev[:1000])
+            elif how == "aos":
+                rec.set_events(ev)
+            elif how == "soa":
+                L = capi.lib()
+                rc = L.jpet_strip_set_events_soa(rec._h, soa[0].ctypes.data, soa[1].ctypes.data,
+                                                 soa[2].ctypes.data, len(ev))
+                assert rc == capi.JPET_OK
+            else:
+                rec.set_events_device(dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(),
+                                      len(ev))
+            rec.rho = np.ones((cg.n_y, cg.n_z), np.float32)
+            rec.iterate(1)
+            if how != "aos_small":
+                imgs.append(rec.rho)
+                c = rec.counters()
+                c.pop("iterations_done")
+                cnts.append(c)
+    for img, c in zip(imgs, cnts):
+        assert rel_l2(img, want) < TOL_ITER
+        assert c == cnts[0] and c["n_kernel_calls"] == st["n_kernel_calls"]
