@@ -334,6 +334,12 @@ typedef struct jpet_strip_gen_images {
   int32_t tan_bins; /* planes of tan_map (0 = no map) */
   int32_t reserved;
   int32_t* tan_map;
+  /* --full (phantom_cmd.cpp:206-232,300-333): per written event, in the order
+   * of the responses, the exact (unsmeared) response (z_u, z_d, dl: 3 floats)
+   * and the emission event (x, y, sin phi, cos phi: 4 floats, the layout of
+   * PET2D::Event); room for `capacity` events each, NULL = not wanted */
+  float* exact_responses;
+  float* events;
 } jpet_strip_gen_images;
 
 /* Writes the detected, smeared responses (z_u, z_d, dl) as float triples to

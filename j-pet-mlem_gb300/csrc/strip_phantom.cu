@@ -93,7 +93,9 @@ __device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
 struct Candidate {
   bool emitted, detected;
   float zu, zd, dl;
-  double px, py;  // emission point
+  double px, py;        // emission point
+  float ex_zu, ex_zd, ex_dl;  // exact (unsmeared) response
+  float dir_x, dir_y;   // emission direction (sin phi, cos phi)
 };
 
 // Optional count images of the phantom tool (phantom_cmd.cpp:249-258,289-352):
@@ -104,6 +106,8 @@ struct GenImages {
   int32_t* detected;  // emission points of the detected events
   int32_t* naive;     // points recovered from the smeared responses
   int32_t* tan_map;   // the same, binned also by tangent
+  float* exact;       // exact responses of the written events (3 floats each)
+  float* events;      // their emission events (x, y, dx, dy)
   double x0, y0, s;
   int32_t n_z, n_y, tan_bins;
   // the grid in the reference's float: lower-left corner, pixel size, 2R, the
@@ -147,7 +151,7 @@ __device__ Candidate gen_candidate(const GenParams& p, const GenRegion* __restri
   uint32_t r1[4] = {lo, hi, 1u, 0u};
   philox(r0, p.key0, p.key1);
   philox(r1, p.key0, p.key1);
-  Candidate out{false, false, 0.f, 0.f, 0.f, 0.0, 0.0};
+  Candidate out{false, false, 0.f, 0.f, 0.f, 0.0, 0.0, 0.f, 0.f, 0.f, 0.f, 0.f};
   // region by cumulative weight (phantom.h:183-191: the first cdf >= u)
   const double u_reg = u53(r0[0], r0[1]);
   int k = 0;
@@ -194,6 +198,15 @@ __device__ Candidate gen_candidate(const GenParams& p, const GenRegion* __restri
   const double half = 0.5 * p.L;
   if (!(fabs(zu) < half && fabs(zd) < half)) return out;
   out.detected = true;
+  out.ex_zu = static_cast<float>(zu);
+  out.ex_zd = static_cast<float>(zd);
+  out.ex_dl = static_cast<float>(dl);
+  {
+    double sp, cp;
+    sincos(phi, &sp, &cp);
+    out.dir_x = static_cast<float>(sp);
+    out.dir_y = static_cast<float>(cp);
+  }
   // Box-Muller on two pairs of uniforms (1 - U in (0, 1]) gives the normals
   uint32_t r2[4] = {lo, hi, 2u, 0u};
   uint32_t r3[4] = {lo, hi, 3u, 0u};
@@ -259,6 +272,17 @@ __global__ void __launch_bounds__(kGenThreads) gen_kernel(
         out[3 * di] = c.zu;
         out[3 * di + 1] = c.zd;
         out[3 * di + 2] = c.dl;
+        if (im.exact) {
+          im.exact[3 * di] = c.ex_zu;
+          im.exact[3 * di + 1] = c.ex_zd;
+          im.exact[3 * di + 2] = c.ex_dl;
+        }
+        if (im.events) {
+          im.events[4 * di] = static_cast<float>(c.px);
+          im.events[4 * di + 1] = static_cast<float>(c.py);
+          im.events[4 * di + 2] = c.dir_x;
+          im.events[4 * di + 3] = c.dir_y;
+        }
       }
       if (c.emitted && (count_emissions ? ei < limit : di < limit)) {
         image_add(im.emitted, im, c.px, c.py);
@@ -438,6 +462,10 @@ int jpet_strip_generate(const jpet_strip_geom* geom, const jpet_strip_region* re
     set_call_error("jpet_strip_generate: tan_map needs tan_bins > 0 and the reverse");
     return JPET_ERR_ARGUMENT;
   }
+  if (images && !(images->emitted || images->detected || images->naive || images->tan_map)) {
+    im.exact = images->exact_responses;
+    im.events = images->events;
+  }
   if (images && (images->emitted || images->detected || images->naive || images->tan_map)) {
     if (geom->n_z_pixels <= 0 || geom->n_y_pixels <= 0 || !(geom->pixel_width > 0)) {
       set_call_error("jpet_strip_generate: count images need n_z, n_y and the pixel size");
@@ -448,6 +476,8 @@ int jpet_strip_generate(const jpet_strip_geom* geom, const jpet_strip_region* re
     im.naive = images->naive;
     im.tan_map = images->tan_map;
     im.tan_bins = images->tan_bins;
+    im.exact = images->exact_responses;
+    im.events = images->events;
     im.s = geom->pixel_width;
     im.n_z = geom->n_z_pixels;
     im.n_y = geom->n_y_pixels;
@@ -577,11 +607,19 @@ int jpet_strip_generate_host(const jpet_strip_geom* geom, const jpet_strip_regio
                        static_cast<size_t>(std::max(geom ? geom->n_z_pixels : 0, 0));
   const size_t n_el[4] = {n_pix, n_pix, n_pix,
                           n_pix * static_cast<size_t>(images ? std::max(images->tan_bins, 0) : 0)};
+  float* d_exact = nullptr;
+  float* d_events = nullptr;
   auto release = [&]() {
     cudaFree(d_out);
+    cudaFree(d_exact);
+    cudaFree(d_events);
     for (auto* q : d_img) cudaFree(q);
   };
   e = cudaMalloc(&d_out, static_cast<size_t>(cap) * 3 * sizeof(float));
+  if (e == cudaSuccess && images && images->exact_responses)
+    e = cudaMalloc(&d_exact, static_cast<size_t>(cap) * 3 * sizeof(float));
+  if (e == cudaSuccess && images && images->events)
+    e = cudaMalloc(&d_events, static_cast<size_t>(cap) * 4 * sizeof(float));
   for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
     if (!h_img[k]) continue;
     e = cudaMalloc(&d_img[k], std::max<size_t>(n_el[k], 1) * sizeof(int32_t));
@@ -599,6 +637,8 @@ int jpet_strip_generate_host(const jpet_strip_geom* geom, const jpet_strip_regio
     dim.detected = d_img[1];
     dim.naive = d_img[2];
     dim.tan_map = d_img[3];
+    dim.exact_responses = d_exact;
+    dim.events = d_events;
   }
   int64_t written = 0;
   int rc = jpet_strip_generate(geom, regions, n_regions, n, seed, flags, d_out, cap, &written,
@@ -609,6 +649,12 @@ int jpet_strip_generate_host(const jpet_strip_geom* geom, const jpet_strip_regio
     for (int k = 0; k < 4 && e == cudaSuccess; ++k)
       if (h_img[k]) e = cudaMemcpy(h_img[k], d_img[k], n_el[k] * sizeof(int32_t),
                                    cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && d_exact)
+      e = cudaMemcpy(images->exact_responses, d_exact,
+                     static_cast<size_t>(written) * 3 * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && d_events)
+      e = cudaMemcpy(images->events, d_events, static_cast<size_t>(written) * 4 * sizeof(float),
+                     cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {
       set_call_error(std::string("jpet_strip_generate_host: copy: ") + cudaGetErrorString(e));
       rc = JPET_ERR_CUDA;

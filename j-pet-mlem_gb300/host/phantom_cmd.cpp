@@ -12,8 +12,10 @@
 // of each voxel at --kernel-point), 3D maps of n_z x n_y x tan_bins.  The
 // events follow a deterministic counter-based stream selected by --seed (the
 // reference seeds std::mt19937 per OpenMP thread, so its output is not
-// reproducible).  --no-responses skips the responses file and keeps the rest.
-// Not supported: --full (the reference's extra event dumps) and PNG previews.
+// reproducible).  --no-responses skips the responses file and keeps the rest;
+// --full adds <base>_wo_error and <base>_full_response (the exact responses)
+// and <base>_events (emission point and direction), each with the output's
+// extension and format.  Not supported: PNG previews.
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -123,6 +125,21 @@ void read_phantom(std::istream& in, double scale, std::vector<jpet_strip_region>
   }
 }
 
+// rows of `width` floats, as text lines ("a b c") or raw binary
+void write_floats(const std::string& fn, const std::vector<float>& v, int64_t rows, int width,
+                  bool text) {
+  if (text) {
+    std::ofstream o(fn);
+    for (int64_t i = 0; i < rows; ++i)
+      for (int k = 0; k < width; ++k) o << v[width * i + k] << (k + 1 < width ? ' ' : '\n');
+    if (!o) throw "cannot write " + fn;
+  } else {
+    std::ofstream o(fn, std::ios::binary);
+    o.write(reinterpret_cast<const char*>(v.data()), rows * width * sizeof(float));
+    if (!o) throw "cannot write " + fn;
+  }
+}
+
 const char* nrrd_type(const int32_t*) { return "int"; }
 const char* nrrd_type(const float*) { return "float"; }
 
@@ -154,7 +171,6 @@ int run(int argc, char* argv[]) {
     }
     throw "at least one input phantom description expected, consult --help";
   }
-  if (cl.exist("full")) throw std::string("--full is not supported by this tool");
   const int tan_bins = cl.get_int("tan-bins");
   if (tan_bins < 0) throw "--tan-bins must not be negative";
   double kernel_x = 0, kernel_y = 0;
@@ -212,6 +228,14 @@ int run(int argc, char* argv[]) {
     im.tan_map = tan_map.data();
   }
   std::vector<float> ev(static_cast<size_t>(std::max<uint64_t>(n, 1)) * 3);
+  const bool full = cl.exist("full") && !cl.exist("no-responses");
+  std::vector<float> exact, events;
+  if (full) {
+    exact.resize(ev.size());
+    events.resize(static_cast<size_t>(std::max<uint64_t>(n, 1)) * 4);
+    im.exact_responses = exact.data();
+    im.events = events.data();
+  }
   int64_t written = 0;
   const int32_t flags = (cl.exist("detected") ? JPET_GEN_DETECTED : 0) |
                         (cl.exist("additive") ? JPET_GEN_ADDITIVE : 0);
@@ -245,6 +269,13 @@ int run(int argc, char* argv[]) {
     std::ofstream o(output, std::ios::binary);
     o.write(reinterpret_cast<const char*>(ev.data()), written * 3 * sizeof(float));
     if (!o) throw "cannot write " + output;
+  }
+  if (full) {
+    // phantom_cmd.cpp:210-219,300-333: the same stream format as the responses;
+    // FullResponse is the exact Response for the strip scanner (scanner.h:35,252-254)
+    write_floats(base + "_wo_error" + ext, exact, written, 3, ext == ".txt");
+    write_floats(base + "_full_response" + ext, exact, written, 3, ext == ".txt");
+    write_floats(base + "_events" + ext, events, written, 4, ext == ".txt");
   }
   {
     std::ofstream cfg(base + ".cfg");

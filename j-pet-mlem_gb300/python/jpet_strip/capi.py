@@ -72,6 +72,8 @@ class GenImages(C.Structure):
         ("tan_bins", C.c_int32),
         ("reserved", C.c_int32),
         ("tan_map", C.c_void_p),
+        ("exact_responses", C.c_void_p),
+        ("events", C.c_void_p),
     ]
 
 
@@ -296,25 +298,35 @@ def generate(regions, n: int, radius: float, length: float, sigma_z: float, sigm
 
 def generate_with_images(regions, n: int, geom: "Geometry", seed: int, detected: bool = True,
                          additive: bool = False, origin=(0.0, 0.0), tan_bins: int = 0,
-                         device: int = 0):
+                         full: bool = False, device: int = 0):
     """The phantom tool's outputs through jpet_strip_generate_host: the events
     (float32[k, 3]) and the int32 count images on geom's grid (emitted,
     detected, naive: [n_y, n_z], row 0 the lowest y; tan_map:
-    [tan_bins, n_y, n_z] when tan_bins > 0)."""
+    [tan_bins, n_y, n_z] when tan_bins > 0); with ``full`` also the exact
+    responses (float32[k, 3]) and emission events (float32[k, 4]: x, y, sin
+    phi, cos phi) of the returned events."""
     g = geom.c()
     regs = _regions(regions)
     shape = (geom.n_y, geom.n_z)
     imgs = {k: np.zeros(shape, np.int32) for k in ("emitted", "detected", "naive")}
     if tan_bins > 0:
         imgs["tan_map"] = np.zeros((tan_bins,) + shape, np.int32)
+    out = np.zeros((max(n, 1), 3), np.float32)
+    if full:
+        imgs["exact"] = np.zeros((max(n, 1), 3), np.float32)
+        imgs["events"] = np.zeros((max(n, 1), 4), np.float32)
     im = GenImages(_ptr(imgs["emitted"]), _ptr(imgs["detected"]), _ptr(imgs["naive"]),
                    float(origin[0]), float(origin[1]), int(tan_bins), 0,
-                   _ptr(imgs["tan_map"]) if tan_bins > 0 else None)
-    out = np.zeros((max(n, 1), 3), np.float32)
+                   _ptr(imgs["tan_map"]) if tan_bins > 0 else None,
+                   _ptr(imgs["exact"]) if full else None,
+                   _ptr(imgs["events"]) if full else None)
     written = C.c_int64(0)
     flags = (GEN_DETECTED if detected else 0) | (GEN_ADDITIVE if additive else 0)
     _check(lib().jpet_strip_generate_host(C.byref(g), regs, len(regions), n, seed, flags,
                                           _ptr(out), n, C.byref(written), C.byref(im), device))
+    if full:
+        imgs["exact"] = imgs["exact"][: written.value]
+        imgs["events"] = imgs["events"][: written.value]
     return out[: written.value], imgs
 
 

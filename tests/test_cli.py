@@ -110,9 +110,6 @@ def test_phantom_tool_usage_and_errors(tmp_path):
     (tmp_path / "bad.txt").write_text("hexagon 0 0 1 1 1\n")
     r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "-e", "10", str(tmp_path / "bad.txt")])
     assert r.returncode == 1 and "unknown phantom type: hexagon" in r.stderr
-    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "-e", "10", "--full",
-                     str(tmp_path / "bad.txt")])
-    assert r.returncode == 1 and "not supported" in r.stderr
     golden = os.path.join(ROOT, "tests", "golden", "phantom_three.txt")
     r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "-e", "10", "--tan-bins", "-2",
                      golden])
@@ -147,6 +144,19 @@ def test_phantom_then_reconstruction_tool_chain(tmp_path):
     assert r.returncode == 0, r.stderr
     ev2 = np.loadtxt(tmp_path / "ph2.txt", dtype=np.float32).reshape(-1, 3)
     assert ev2.shape == ev.shape and np.allclose(ev2, ev, rtol=1e-5, atol=1e-3)
+    # --full: exact responses and emission events beside the smeared responses
+    r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "--n-z-pixels", "200",
+                     "--n-y-pixels", "180", "--s-z", "10", "--s-dl", "42", "-e", "20000",
+                     "--seed", "7", "--full", "-o", str(tmp_path / "fu.bin"), golden])
+    assert r.returncode == 0, r.stderr
+    sm = np.fromfile(tmp_path / "fu.bin", np.float32).reshape(-1, 3)
+    ex = np.fromfile(tmp_path / "fu_wo_error.bin", np.float32).reshape(-1, 3)
+    fr = np.fromfile(tmp_path / "fu_full_response.bin", np.float32).reshape(-1, 3)
+    evs = np.fromfile(tmp_path / "fu_events.bin", np.float32).reshape(-1, 4)
+    assert len(sm) == len(ex) == len(fr) == len(evs) > 0 and np.array_equal(ex, fr)
+    assert np.all(np.abs(ex[:, :2]) < 500.0)
+    assert abs(float(np.std(sm[:, 0] - ex[:, 0])) - 10.0) < 0.5
+    assert np.allclose(np.hypot(evs[:, 2], evs[:, 3]), 1.0, atol=1e-6)
     # --no-responses: images and .cfg only
     r = run_phantom(["-r", "450", "-l", "1000", "-p", "5", "--n-z-pixels", "200",
                      "--n-y-pixels", "180", "--s-z", "10", "--s-dl", "42", "-e", "20000",

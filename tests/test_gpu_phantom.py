@@ -148,3 +148,28 @@ def test_tan_kernel_map_matches_the_oracle(divide):
     assert float(np.max(np.abs(got - want))) <= 2e-6 * scale
     big = want > 1e-3 * scale
     np.testing.assert_allclose(got[big], want[big], rtol=2e-6)
+
+
+def test_full_outputs_are_the_exact_projection_of_the_emission_events():
+    """--full outputs: each emission event (x, y, sin phi, cos phi) projects to
+    its exact response (scanner.h:107-113), which lies on the scintillators
+    (scanner.h:208-213); the written response is that response plus the
+    Gaussian smearing (sigma_z, sigma_dl); the events and responses keep the
+    order and count of the plain stream."""
+    ell = phantom.three_ellipse_phantom()
+    geom = capi.Geometry(R, L, 180, 200, 5.0, 10.0, 42.0)
+    ev, im = capi.generate_with_images(ell, 200000, geom, seed=4, full=True)
+    ex, evs = im["exact"].astype(np.float64), im["events"].astype(np.float64)
+    assert ex.shape == (len(ev), 3) and evs.shape == (len(ev), 4)
+    x, y, sx, cx = evs.T
+    assert np.allclose(sx * sx + cx * cx, 1.0, atol=1e-6)
+    t = sx / cx
+    np.testing.assert_allclose(ex[:, 0], x + (R - y) * t, rtol=1e-5, atol=2e-3)
+    np.testing.assert_allclose(ex[:, 1], x - (R + y) * t, rtol=1e-5, atol=2e-3)
+    np.testing.assert_allclose(ex[:, 2], -2 * y * np.sqrt(t * t + 1), rtol=1e-5, atol=2e-3)
+    assert np.all(np.abs(ex[:, :2]) < L / 2)
+    d = ev.astype(np.float64) - ex
+    assert abs(d[:, 0].std() - 10.0) < 0.1 and abs(d[:, 1].std() - 10.0) < 0.1
+    assert abs(d[:, 2].std() - 42.0) < 0.4 and abs(d.mean(0)).max() < 0.3
+    plain = capi.generate(ell, 200000, R, L, 10.0, 42.0, seed=4)
+    assert np.array_equal(plain, ev)
