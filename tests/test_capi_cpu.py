@@ -52,6 +52,10 @@ def test_create_rejects_bad_geometry_without_device():
     assert b"n_y_pixels" in L.jpet_strip_last_error(None)
     g = capi.Geometry(450, 1000, 180, 200, -5, 10, 42).c()
     assert L.jpet_strip_create(C.byref(g), None, C.byref(h)) == capi.JPET_ERR_ARGUMENT
+    # the reference's pixel indices are short (scanner.h:142-144): at most 32767
+    g = capi.Geometry(450, 1000, 10, 32768, 5, 10, 42).c()
+    assert L.jpet_strip_create(C.byref(g), None, C.byref(h)) == capi.JPET_ERR_ARGUMENT
+    assert b"32767" in L.jpet_strip_last_error(None)
     assert L.jpet_strip_create(C.byref(g), None, None) == capi.JPET_ERR_ARGUMENT
     assert L.jpet_strip_destroy(None) == 0
 

@@ -409,3 +409,27 @@ def test_upload_paths_agree(golden):
     for img, c in zip(imgs, cnts):
         assert rel_l2(img, want) < TOL_ITER
         assert c == cnts[0] and c["n_kernel_calls"] == st["n_kernel_calls"]
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_fine_pixels_with_boxes_beyond_every_shape(variant):
+    """0.5 mm pixels with sigma 10/42: boxes of ~250 x 85 pixels exceed every
+    register shape and most exceed the shared-memory window, so the events take
+    the queued reference-order path and the global large-box path; the image
+    and counters are still the reference's."""
+    ell = phantom.random_ellipse_phantom(seed=12, half_z=120.0, half_y=90.0, centre_z=60.0,
+                                         centre_y=50.0, axes=(5.0, 60.0))
+    ev = phantom.generate_events(ell, 1500, 450.0, 1000.0, 10.0, 42.0, seed=12)
+    args = (450.0, 1000.0, 400, 500, 0.5, 10.0, 42.0)
+    cg, og = capi.Geometry(*args), O.Geometry(*args)
+    want, st = O.mlem_f(og, ev, 2, threads=8)
+    with capi.StripReconstruction(cg, variant=variant) as rec:
+        rec.set_events(ev)
+        rec.iterate(2)
+        got = rec.rho
+        cnt = rec.counters()
+    assert rel_l2(got, want) < TOL_ITER
+    assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
+    assert cnt["n_contributing"] == st["n_contributing"]
+    if variant != capi.VARIANT_EXACT:
+        assert cnt["n_oversize"] + cnt["n_exact_path"] > 0, cnt
