@@ -365,6 +365,22 @@ def gb300_arm(args, wl, world, rank, local):
                     "sfu_frac": evals_per_s / ex2_peak,
                     "shared_atomic_frac": evals_per_s / atom_peak,
                     "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_kind}
+        if args.variant == 0:
+            traffic = profile_traffic(n_events)
+            insts = profile_traffic(n_events, "warp_instructions_per_launch")
+            if traffic:
+                roofline["hbm_achieved_gbs"] = traffic / (kernel_ms * 1e-3) / 1e9
+                roofline["hbm_frac"] = roofline["hbm_achieved_gbs"] / hbm
+            sm_mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz")
+            if insts and sm_mhz:
+                # 4 warp schedulers per SM issue one warp instruction per clock each
+                n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+                issue_peak = 4 * n_sm * sm_mhz * 1e6
+                roofline["issue_frac"] = insts / (kernel_ms * 1e-3) / issue_peak
+                roofline["issue_note"] = ("warp instructions per launch (ncu count of the "
+                                          "committed profile, scaled by events) / kernel time / "
+                                          "(4 schedulers x SMs x median SM clock): the roof "
+                                          "that binds this instruction-bound kernel")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "kernel": {"variant": ["fast", "exact", "warp"][args.variant],
@@ -397,15 +413,16 @@ def gb300_arm(args, wl, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
-def profile_traffic(n_events):
-    """DRAM bytes per iteration-kernel launch from the committed ncu summary of
-    the row-owned kernel (dram__bytes_read.sum + dram__bytes_write.sum of one
-    captured launch), scaled from the captured event count to n_events."""
+def profile_traffic(n_events, key="dram_bytes_per_launch"):
+    """DRAM bytes (or warp instructions, key "warp_instructions_per_launch") per
+    iteration-kernel launch from the committed ncu summary of the row-owned
+    kernel (dram__bytes_read.sum + dram__bytes_write.sum, smsp__inst_executed.sum
+    of one captured launch), scaled from the captured event count to n_events."""
     path = os.path.join(ROOT, "profiles", "iterate_rows_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
-        return d["dram_bytes_per_launch"] * n_events / d["events"]
+        return d[key] * n_events / d["events"]
     except (OSError, KeyError, ValueError, ZeroDivisionError):
         return None
 
