@@ -332,8 +332,8 @@ __device__ __forceinline__ void rows_chunk(
       // their pass below changes no pixel, so it runs without a branch
       const float inv = __shfl_sync(kFull, inv_l, j);
       // Branch-free read-modify-write of the pixel pair: the pair is always
-      // loaded (inside the window), each pixel stored only if it received a
-      // contribution, so no lane writes a pixel outside its event's rows.
+      // loaded (inside the window) and stored only if one of its pixels
+      // received a contribution, so no lane writes outside its event's rows.
       if (ACC == kAccFixed) {
         // q = floor(v 2^22 + U), U uniform in [0, 1) per event: E[q] = v 2^22
         const uint32_t key = hash32(static_cast<uint32_t>(c.start + b * E + j) ^ seed);
@@ -374,17 +374,16 @@ __device__ __forceinline__ void rows_chunk(
               const float2 err = __fadd2_rn(fsub2(o, fsub2(n, bp)), fsub2(v, bp));
               const float2 co = *reinterpret_cast<const float2*>(cp);
               const float2 cn = __fadd2_rn(co, err);
-              if (kr.x != 0.0f) {
-                op[0] = n.x;
-                cp[0] = cn.x;
-              }
-              if (kr.y != 0.0f) {
-                op[1] = n.y;
-                cp[1] = cn.y;
+              // a pixel without contribution keeps n = o and err = 0, cn = co
+              if (kr.x != 0.0f || kr.y != 0.0f) {
+                *reinterpret_cast<float2*>(op) = n;
+                *reinterpret_cast<float2*>(cp) = cn;
               }
             } else {
-              if (kr.x != 0.0f) op[0] = n.x;
-              if (kr.y != 0.0f) op[1] = n.y;
+              // one 8-byte store when either pixel received a contribution: the
+              // other pixel of the pair gets o + 0 = o (it lies in the same row,
+              // owned by this warp, inside the window's pitch)
+              if (kr.x != 0.0f || kr.y != 0.0f) *reinterpret_cast<float2*>(op) = n;
             }
           }
         }
