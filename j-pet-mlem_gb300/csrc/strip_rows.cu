@@ -246,6 +246,9 @@ __device__ __forceinline__ void rows_chunk(
     const float2* sp = stage_pq(buf);
     float2 cache[E][RS][SW];
     int base[E][RS];
+    // column bound of the row's pixel pairs: a pair starting at k0 holds a
+    // pixel of the event iff k0 < bound (0 for rows outside the event)
+    int bound[E][RS];
     unsigned fits_mask = 0;
     DenT dsum[E];
     // ---- forward: this warp's rows of every event of the batch
@@ -275,6 +278,7 @@ __device__ __forceinline__ void rows_chunk(
         const int end = lead + w;
         const int bse = static_cast<int>(en & 0xFFFFFEu) + 2 * gl;
         base[j][rs] = bse;
+        bound[j][rs] = w > 0 ? end : 0;
         const float2 p2 = make_float2(pqv.x, pqv.x), q2 = make_float2(pqv.y, pqv.y);
 #pragma unroll
         for (int s = 0; s < SW; ++s) {
@@ -383,7 +387,7 @@ __device__ __forceinline__ void rows_chunk(
               // one 8-byte store when either pixel received a contribution: the
               // other pixel of the pair gets o + 0 = o (it lies in the same row,
               // owned by this warp, inside the window's pitch)
-              if (kr.x != 0.0f || kr.y != 0.0f) *reinterpret_cast<float2*>(op) = n;
+              if (2 * gl + kSweep * s < bound[j][rs]) *reinterpret_cast<float2*>(op) = n;
             }
           }
         }
