@@ -173,3 +173,25 @@ def test_oracle_tan_maps_are_consistent():
     _, row, col = np.unravel_index(np.argmax(m), m.shape)
     # grid row 0 is the lowest y: pixel centre -450 + 10 (row + 0.5)
     assert abs(-500 + 10 * (col + 0.5) - 20.0) <= 10 and abs(-450 + 10 * (row + 0.5) + 10.0) <= 10
+
+
+def test_header_compiles_as_c99_and_cxx11(tmp_path):
+    """include/jpet_strip.h is a plain C header (what cgo, JNI or a C caller
+    includes) and also valid C++11 (the reference's language level)."""
+    import shutil
+    import subprocess
+
+    src = tmp_path / "use.c"
+    src.write_text('#include <string.h>\n#include "jpet_strip.h"\n'
+                   "int main(void) {\n"
+                   "  jpet_strip_opts o; jpet_strip_default_opts(&o);\n"
+                   "  jpet_strip_gen_images im; memset(&im, 0, sizeof im);\n"
+                   "  return o.mode + im.tan_bins;\n}\n")
+    inc = os.path.join(ROOT, "include")
+    for cc, std, lang in (("gcc", "-std=c99", "c"), ("g++", "-std=c++11", "c++")):
+        if not shutil.which(cc):
+            pytest.skip(f"{cc} not available")
+        r = subprocess.run([cc, std, "-Wall", "-Wextra", "-Werror", "-x", lang, "-I", inc, "-c",
+                            str(src), "-o", str(tmp_path / f"use_{lang}.o")],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
