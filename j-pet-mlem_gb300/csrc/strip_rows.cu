@@ -356,8 +356,10 @@ __device__ __forceinline__ void rows_chunk(
             const uint32_t q1 = __float_as_uint(x.y) - 0x4B400000u;
             uint32_t* op = oq + base[j][rs] + kSweep * s;
             const uint2 o = *reinterpret_cast<const uint2*>(op);
-            if (kr.x != 0.0f) op[0] = o.x + q0;
-            if (kr.y != 0.0f) op[1] = o.y + q1;
+            // a zero contribution quantises to q = 0 (|dither| <= 0.5 rounds to
+            // the magic constant, ties to even), so the pair is stored whole
+            if (2 * gl + kSweep * s < bound[j][rs])
+              *reinterpret_cast<uint2*>(op) = make_uint2(o.x + q0, o.y + q1);
           }
         }
       } else {
@@ -379,7 +381,7 @@ __device__ __forceinline__ void rows_chunk(
               const float2 co = *reinterpret_cast<const float2*>(cp);
               const float2 cn = __fadd2_rn(co, err);
               // a pixel without contribution keeps n = o and err = 0, cn = co
-              if (kr.x != 0.0f || kr.y != 0.0f) {
+              if (2 * gl + kSweep * s < bound[j][rs]) {
                 *reinterpret_cast<float2*>(op) = n;
                 *reinterpret_cast<float2*>(cp) = cn;
               }
