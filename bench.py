@@ -383,7 +383,7 @@ def gb300_arm(args, wl, world, rank, local):
                                           "that binds this instruction-bound kernel")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "kernel": {"variant": ["fast", "exact", "warp"][args.variant],
+        "kernel": {"variant": ["fast", "exact", "warp", "rows"][args.variant],
                    "raster_shape": args.raster_shape, "block_threads": args.block_threads,
                    "precision": ["fp32", "compensated", "fp64_den", "fixed"][args.precision]},
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

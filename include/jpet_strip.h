@@ -75,12 +75,17 @@ typedef struct jpet_strip_geom {
                                         summed with integer shared atomics; FP64 image */
 
 /* iteration kernel */
-#define JPET_VARIANT_FAST 0  /* exp2-form kernel, packed f32x2, register-cached K*rho; image
-                                rows owned by warps, no shared-memory atomics (default) */
+#define JPET_VARIANT_FAST 0  /* default.  FP32: batch-union kernel -- batches of <= 8 similar
+                                events share one lane-to-pixel map, rho is read and the
+                                back-projection written once per batch, exp2-form kernel with
+                                packed f32x2, per-row coefficients regenerated on chip; other
+                                precisions: the ROWS kernel */
 #define JPET_VARIANT_EXACT 1 /* every pixel evaluated in the reference's operation order */
-#define JPET_VARIANT_WARP 2  /* as FAST with one warp per event and shared-memory atomics */
+#define JPET_VARIANT_WARP 2  /* one warp per event, shared-memory atomics */
+#define JPET_VARIANT_ROWS 3  /* row-owned kernel: image rows owned by warps, one event at a
+                                time per row, per-row coefficients precomputed at set-up */
 
-/* register-cache shape of the FAST kernel: G lanes per image row x passes of
+/* register-cache shape of the ROWS kernel: G lanes per image row x passes of
  * 256/G event rows x sweeps of 2G columns (0 = chosen from the event boxes) */
 #define JPET_RASTER_AUTO 0
 #define JPET_RASTER_8x1x1 1 /* <= 32 rows, <= 15 columns */
@@ -97,8 +102,9 @@ typedef struct jpet_strip_opts {
   int32_t precision;    /* JPET_PRECISION_* */
   int32_t tile_w;       /* image tile width in pixels, 0 = chosen by the tuner */
   int32_t tile_h;       /* image tile height in pixels, 0 = chosen by the tuner */
-  int32_t block_threads;/* threads per CTA of the iteration kernel, 0 = default (128 for
-                           the FAST kernel, which also takes 256; 256 otherwise) */
+  int32_t block_threads;/* threads per CTA of the iteration kernel, 0 = default (256 for
+                           the FP32 FAST kernel: 8 events per batch; 128 for the ROWS kernel;
+                           both take 128 or 256; 256 otherwise) */
   int32_t variant;      /* JPET_VARIANT_*; the GPU-reference mode always runs EXACT */
   int32_t raster_shape; /* JPET_RASTER_*; events outside the shape take the exact path */
   int32_t reserved[8];  /* must be zero */

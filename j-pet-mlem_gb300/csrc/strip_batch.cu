@@ -225,12 +225,15 @@ int jpet_strip_batch_create(int32_t n, const jpet_strip_geom* geoms, const jpet_
   jpet_strip_opts o;
   jpet_strip_default_opts(&o);
   if (opts) o = *opts;
-  if (o.mode != JPET_MODE_CPU_REFERENCE || o.variant != JPET_VARIANT_FAST ||
+  if (o.mode != JPET_MODE_CPU_REFERENCE ||
+      (o.variant != JPET_VARIANT_FAST && o.variant != JPET_VARIANT_ROWS) ||
       o.precision != JPET_PRECISION_FP32) {
     set_call_error("jpet_strip_batch_create: batches run the FP32 row-owned kernel "
-                   "(CPU-reference mode, FAST variant)");
+                   "(CPU-reference mode, FAST or ROWS variant)");
     return JPET_ERR_UNSUPPORTED;
   }
+  // every instance is a handle of the row-owned kernel
+  o.variant = JPET_VARIANT_ROWS;
   auto* b = new jpet_strip_batch();
   b->device = o.device;
   cudaError_t e = cudaSetDevice(o.device);

@@ -79,8 +79,14 @@ struct jpet_strip {
   DevBuf<float2> row_pq;     // per-row exponent coefficients of the row-owned kernel
   DevBuf<uint32_t> row_pk;   // per-row packed window offset / parity / width
   DevBuf<uint32_t> ev_pk;    // per-event packed window row / box rows / fits
+  DevBuf<uint64_t> sort_keys;     // set-up sort: keys (input, output)
+  DevBuf<int32_t> sort_idx;       // set-up sort: event indices (input, output)
+  DevBuf<unsigned char> sort_tmp; // set-up sort: radix-sort scratch
+  DevBuf<uint32_t> batches;       // batch-union kernel: batch words per chunk
+  DevBuf<unsigned char> ev_const; // batch-union kernel: per-event constants
   FastConst fc{};
   bool use_fast = false;
+  bool use_union = false;
   bool counters_valid = false;
   unsigned long long table_kernel_calls = 0;
   DevBuf<unsigned long long> box_pixels;
@@ -191,10 +197,14 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
                    Tiling& t) {
   // window pixels per array (rho, out): 12288 (~100 KiB per CTA, 2 CTAs per SM)
   // for 256-thread CTAs; 6144 (~55 KiB, 4 CTAs per SM) for the row-owned
-  // kernel's 128-thread CTAs
-  const bool rows4 = o.mode == JPET_MODE_CPU_REFERENCE && o.variant == JPET_VARIANT_FAST &&
-                     o.block_threads != 256;
-  const int budget_px = rows4 ? 6144 : 12288;
+  // kernel's 128-thread CTAs and for the batch-union kernel (~66 KiB with its
+  // batch records, 2 CTAs of 256 threads per SM)
+  const bool fast = o.mode == JPET_MODE_CPU_REFERENCE &&
+                    (o.variant == JPET_VARIANT_FAST || o.variant == JPET_VARIANT_ROWS);
+  const bool union_fp32 = fast && o.variant == JPET_VARIANT_FAST &&
+                          o.precision == JPET_PRECISION_FP32;
+  const bool rows4 = fast && o.block_threads != 256;
+  const int budget_px = (rows4 || union_fp32) ? 6144 : 12288;
   auto pct = [&](const std::vector<int32_t>& h, double keep) {
     int64_t tail = static_cast<int64_t>(std::floor((1.0 - keep) * n_nonempty));
     int64_t acc = 0;
@@ -231,7 +241,9 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
   t.n_tiles_x = (n_z + tw - 1) / tw;
   t.n_tiles_y = (n_y + th - 1) / th;
   t.chunk_events = 512;
-  t.threads = o.block_threads > 0 ? o.block_threads : (rows4 ? 128 : 256);
+  // the FP32 batch-union kernel (FAST variant) defaults to 256-thread CTAs
+  // (8 events per batch); the row-owned kernel to 128
+  t.threads = o.block_threads > 0 ? o.block_threads : (union_fp32 ? 256 : (rows4 ? 128 : 256));
   t.group = 32;
   // one spare entry per event for its widest row; a multiple of 8 entries so
   // that every event's table starts on a 16-byte boundary
@@ -348,12 +360,20 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
   JPET_CUDA(h, h->sorted_box.alloc(std::max(acc, 1)), "cudaMalloc(sorted events)");
   JPET_CUDA(h, h->over_geom.alloc(std::max(n_over, 1)), "cudaMalloc(large events)");
   JPET_CUDA(h, h->over_box.alloc(std::max(n_over, 1)), "cudaMalloc(large events)");
-  JPET_CUDA(h, cudaMemsetAsync(h->small.p + 1, 0, sizeof(int32_t), s), "memset");
-  JPET_CUDA(h, launch_scatter_events(n, h->ev_geom.p, h->ev_box.p, h->ev_key.p, h->tile_offset.p,
-                                     h->tile_cursor.p, h->sorted_geom.p, h->sorted_box.p,
-                                     h->small.p + 1, h->over_geom.p, h->over_box.p, s),
-            "scatter_events launch");
+  if (n > 0) {
+    // tile, then box corner inside the tile, then tan (strip_sort.cu)
+    const size_t tmp = sort_temp_bytes(n);
+    JPET_CUDA(h, h->sort_keys.alloc(2 * static_cast<size_t>(n)), "cudaMalloc(sort keys)");
+    JPET_CUDA(h, h->sort_idx.alloc(2 * static_cast<size_t>(n)), "cudaMalloc(sort indices)");
+    JPET_CUDA(h, h->sort_tmp.alloc(std::max<size_t>(tmp, 1)), "cudaMalloc(sort scratch)");
+    JPET_CUDA(h, sort_events(t, n, h->ev_geom.p, h->ev_box.p, h->sort_keys.p, h->sort_idx.p,
+                             h->sort_tmp.p, tmp, acc, n_over, h->sorted_geom.p, h->sorted_box.p,
+                             h->over_geom.p, h->over_box.p, s),
+              "event sort");
+  }
   h->use_fast = h->opts.mode == JPET_MODE_CPU_REFERENCE && h->opts.variant != JPET_VARIANT_EXACT;
+  h->use_union = h->use_fast && h->opts.variant == JPET_VARIANT_FAST &&
+                 h->opts.precision == JPET_PRECISION_FP32;
   h->table_kernel_calls = 0;
   if (h->use_fast && acc > 0) {
     JPET_CUDA(h, h->row_table.alloc(static_cast<size_t>(acc) * t.row_stride),
@@ -362,7 +382,16 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
     JPET_CUDA(h, launch_row_tables(h->g, t, acc, h->sorted_geom.p, h->sorted_box.p,
                                    h->row_table.p, h->box_pixels.p, s),
               "row_table launch");
-    if (h->opts.variant == JPET_VARIANT_FAST) {
+    if (h->use_union) {
+      JPET_CUDA(h, h->batches.alloc(static_cast<size_t>(acc)), "cudaMalloc(batches)");
+      JPET_CUDA(h, h->ev_const.alloc(static_cast<size_t>(acc) * union_event_bytes()),
+                "cudaMalloc(event constants)");
+      JPET_CUDA(h, launch_union_setup(h->g, h->fc, t, h->chunks.p, h->n_chunks, acc,
+                                      h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
+                                      h->ev_const.p, h->batches.p, s),
+                "batch formation launch");
+      JPET_CUDA(h, union_prepare_kernel(t), "batch-union kernel attributes");
+    } else if (h->opts.variant == JPET_VARIANT_FAST || h->opts.variant == JPET_VARIANT_ROWS) {
       JPET_CUDA(h, h->row_pq.alloc(static_cast<size_t>(acc) * t.row_stride),
                 "cudaMalloc(row coefficients)");
       JPET_CUDA(h, h->row_pk.alloc(static_cast<size_t>(acc) * t.row_stride),
@@ -377,11 +406,14 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
                                  sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
               "copy counter");
   }
-  JPET_CUDA(h, cudaStreamSynchronize(s), "scatter_events");
-  // unsorted copies are no longer needed
+  JPET_CUDA(h, cudaStreamSynchronize(s), "prepare events");
+  // unsorted copies and sort buffers are no longer needed
   h->ev_geom.release();
   h->ev_box.release();
   h->ev_key.release();
+  h->sort_keys.release();
+  h->sort_idx.release();
+  h->sort_tmp.release();
   h->events_ready = true;
   h->counters_valid = false;
   return JPET_OK;
@@ -424,9 +456,9 @@ int handle_batch_view(jpet_strip* h, BatchInstance* v, std::string& why) {
     why = "events not set";
     return JPET_ERR_STATE;
   }
-  if (!h->use_fast || h->opts.variant != JPET_VARIANT_FAST ||
+  if (!h->use_fast || h->opts.variant != JPET_VARIANT_ROWS ||
       h->opts.precision != JPET_PRECISION_FP32) {
-    why = "batched instances run the FP32 row-owned kernel (CPU-reference mode, FAST variant)";
+    why = "batched instances run the FP32 row-owned kernel (CPU-reference mode, ROWS variant)";
     return JPET_ERR_UNSUPPORTED;
   }
   v->g = h->g;
@@ -500,11 +532,12 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
     return JPET_ERR_ARGUMENT;
   }
   if (o.variant != JPET_VARIANT_FAST && o.variant != JPET_VARIANT_EXACT &&
-      o.variant != JPET_VARIANT_WARP) {
+      o.variant != JPET_VARIANT_WARP && o.variant != JPET_VARIANT_ROWS) {
     g_create_error = "unknown kernel variant";
     return JPET_ERR_ARGUMENT;
   }
-  if (o.mode == JPET_MODE_CPU_REFERENCE && o.variant == JPET_VARIANT_FAST &&
+  if (o.mode == JPET_MODE_CPU_REFERENCE &&
+      (o.variant == JPET_VARIANT_FAST || o.variant == JPET_VARIANT_ROWS) &&
       o.block_threads != 0 && o.block_threads != 128 && o.block_threads != 256) {
     g_create_error = "the row-owned kernel runs 128- or 256-thread CTAs";
     return JPET_ERR_ARGUMENT;
@@ -607,6 +640,11 @@ int jpet_strip_destroy(jpet_strip_t* h) {
   h->row_pq.release();
   h->row_pk.release();
   h->ev_pk.release();
+  h->sort_keys.release();
+  h->sort_idx.release();
+  h->sort_tmp.release();
+  h->batches.release();
+  h->ev_const.release();
   h->box_pixels.release();
   h->nll_acc.release();
   h->nll_grad_tmp.release();
@@ -692,7 +730,13 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
                        : h->opts.precision == JPET_PRECISION_FIXED    ? kPrecisionFixed
                                                                       : kPrecisionFloat;
       const uint32_t seed = 0x9E3779B9u * static_cast<uint32_t>(h->iterations_done + 1);
-      if (h->opts.variant == JPET_VARIANT_WARP) {
+      if (h->use_union) {
+        JPET_CUDA(h, launch_iterate_union(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
+                                          h->sorted_geom.p, h->sorted_box.p, h->ev_const.p,
+                                          h->row_table.p, h->batches.p, h->rho.p, h->out.p,
+                                          h->counters.p, s),
+                  "iteration kernel launch");
+      } else if (h->opts.variant == JPET_VARIANT_WARP) {
         JPET_CUDA(h, launch_iterate_fast(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
                                          h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
                                          h->rho.p, h->out.p, h->out64.p, h->counters.p, prec,

@@ -28,6 +28,8 @@ struct Chunk {
   int32_t start;  // first event in the sorted event arrays
   int32_t count;  // number of events
   int32_t ox, oy; // window origin (pixel column, row)
+  int32_t n_batches;  // batch-union kernel: batches of the chunk (set-up)
+  int32_t n_exact;    // batch-union kernel: events rasterised in the reference's order
 };
 
 // Window and tiling parameters chosen at set_events time.
@@ -141,6 +143,30 @@ cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Til
                                 const uint32_t* rows, const float2* pq, const float* rho,
                                 float* out, double* out64, DevCounters* counters,
                                 int precision, uint32_t seed, cudaStream_t s);
+// Set-up order of the events (strip_sort.cu): radix sort by tile, box corner
+// and tan, then a gather into the tile-sorted and oversize arrays.
+size_t sort_temp_bytes(int64_t n);
+cudaError_t sort_events(const Tiling& t, int64_t n, const float4* ev_geom, const short4* ev_box,
+                        uint64_t* keys, int32_t* idx, void* temp, size_t temp_bytes,
+                        int64_t n_tile_events, int64_t n_over, float4* sorted_geom,
+                        short4* sorted_box, float4* over_geom, short4* over_box,
+                        cudaStream_t s);
+// Batch-union kernel (strip_union.cu): per-event constants and batches of up
+// to 4 (128-thread CTAs) or 8 (256-thread CTAs) similar events per chunk
+// (set-up), and the FP32 iteration over them.
+size_t union_event_bytes();
+size_t union_smem_bytes(const Tiling& t);
+bool union_split_exponent(const DevGeom& g, const FastConst& fc);
+cudaError_t union_prepare_kernel(const Tiling& t);
+cudaError_t launch_union_setup(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                               Chunk* chunks, int32_t n_chunks, int32_t n_events,
+                               const float4* ev_geom, const short4* ev_box, const uint16_t* rows,
+                               void* ev_const, uint32_t* batches, cudaStream_t s);
+cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
+                                 const short4* ev_box, const void* ev_const,
+                                 const uint16_t* rows, const uint32_t* batches, const float* rho,
+                                 float* out, DevCounters* counters, cudaStream_t s);
 cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint16_t* rows, const float* rho,

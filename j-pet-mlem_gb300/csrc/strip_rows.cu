@@ -35,6 +35,7 @@
 #include "strip_fast_common.cuh"
 #include "strip_internal.h"
 #include "strip_raster.cuh"
+#include "strip_async.cuh"
 
 namespace jpet {
 namespace {
@@ -46,19 +47,6 @@ __device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
   return __fadd2_rn(a, make_float2(-b.x, -b.y));
 }
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
-  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
-  const int n = valid ? 16 : 0;
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(n)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.wait_all;" ::: "memory");
-}
-
 // Staging buffer of one batch: E packed event words, E packed row tables and E
 // rows of exponent coefficients (float2), each part 16-byte aligned.
 __host__ __device__ inline int rows_stage_tab(int e) { return (e * 4 + 15) & ~15; }
@@ -67,76 +55,6 @@ __host__ __device__ inline int rows_stage_pq(int e, int stride) {
 }
 __host__ __device__ inline int rows_stage_bytes(int e, int stride) {
   return (rows_stage_pq(e, stride) + e * stride * 8 + 15) & ~15;
-}
-
-__device__ __forceinline__ void cp_async4(void* dst, const void* src, bool valid) {
-  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
-  const int n = valid ? 4 : 0;
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(n)
-               : "memory");
-}
-
-// Sum over the 32 lanes of E per-lane values, transposed: afterwards lane l
-// holds the warp total of value rows_lane_event<E>(l) (lanes that differ only
-// in the low bits hold the same total).
-template <int E>
-__device__ __forceinline__ float rows_transpose_sum(float (&v)[E]) {
-  const int lane = threadIdx.x & 31;
-  int n = E;
-  int off = 16;
-#pragma unroll
-  for (int step = 0; step < 5; ++step) {
-    if (n > 1) {
-      const bool hi = (lane & off) != 0;
-#pragma unroll
-      for (int k = 0; k < E / 2; ++k) {
-        if (k < n / 2) {
-          const float send = hi ? v[k] : v[k + n / 2];
-          const float keep = hi ? v[k + n / 2] : v[k];
-          v[k] = keep + __shfl_xor_sync(kFull, send, off);
-        }
-      }
-      n /= 2;
-    } else {
-      v[0] += __shfl_xor_sync(kFull, v[0], off);
-    }
-    off >>= 1;
-  }
-  return v[0];
-}
-template <int E>
-__device__ __forceinline__ double rows_transpose_sum(double (&v)[E]) {
-  const int lane = threadIdx.x & 31;
-  int n = E;
-  int off = 16;
-#pragma unroll
-  for (int step = 0; step < 5; ++step) {
-    if (n > 1) {
-      const bool hi = (lane & off) != 0;
-#pragma unroll
-      for (int k = 0; k < E / 2; ++k) {
-        if (k < n / 2) {
-          const double send = hi ? v[k] : v[k + n / 2];
-          const double keep = hi ? v[k + n / 2] : v[k];
-          v[k] = keep + __shfl_xor_sync(kFull, send, off);
-        }
-      }
-      n /= 2;
-    } else {
-      v[0] += __shfl_xor_sync(kFull, v[0], off);
-    }
-    off >>= 1;
-  }
-  return v[0];
-}
-// the value index lane l holds after rows_transpose_sum: its bits 4, 3, ... in turn
-template <int E>
-__device__ __forceinline__ int rows_lane_event(int lane) {
-  return E == 8 ? ((lane >> 2) & 7) : (E == 4 ? ((lane >> 3) & 3) : ((lane >> 4) & 1));
-}
-template <int E>
-__device__ __forceinline__ bool rows_lane_writes(int lane) {
-  return (lane & (32 / E - 1)) == 0;
 }
 
 // One chunk of events of one tile on one CTA (the whole body of the kernel;

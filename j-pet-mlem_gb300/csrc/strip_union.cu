@@ -1,0 +1,603 @@
+// Batch-union MLEM iteration kernel for the CPU-reference semantics (the
+// default FP32 kernel), and the set-up passes that feed it.
+//
+// Events are sorted by image tile, then by their box corner inside the tile and
+// by tan (strip_sort.cu), so neighbouring events in a chunk have nearly the same
+// box and the same in-ellipse rows.  At set-up, union_batches_kernel groups each
+// chunk's events greedily into batches of up to E consecutive events whose
+// union -- per window row, from the smallest first column (rounded down to
+// even) to the largest last column -- spans at most 64 rows and 32 columns.  An
+// event that does not fit that rectangle on its own is rasterised in the
+// reference's order instead (the exact path); union_events_kernel stores each
+// event's constants (y, tan, exponent coefficients, window-relative box).
+//
+// The iteration kernel runs one CTA of NW warps per chunk (E = NW events per
+// batch), with the rho and back-projection windows of the tile in shared
+// memory.  For a batch, union row r belongs to the 4 lanes (gid) of one warp,
+// lane gl owning the pixel pairs 2 gl + 8 s (s < 4) of the row from its even
+// start column: the SAME pixels for every event of the batch.  So rho is read
+// once per batch, each event's K rho stays in registers, and the
+// back-projection adds sum_e K_e rho inv_e to each owned pixel pair with one
+// shared-memory read-modify-write per batch (not per event); no pixel has two
+// writers in a batch and no atomics are issued.  The per-(event, row)
+// exponent coefficients and column masks of batch b + 1 are computed by all
+// threads while batch b is in flight (double-buffered), so a batch costs one
+// CTA barrier (the one that publishes the denominators).
+//
+// Kernel value (src/2d/strip/gaussian_kernel.h:51-79, rewritten as in
+// strip_fast.cu): along a row the exponent of K / K_ref is p + q j + c j^2 with
+// c = kz pw^2.  With j counted from the union row's even start column and
+// jc = j - 16, K = 2^(p' + q' jc) * 2^(c jc^2); the second factor is the same
+// for every event, row and batch, so where it stays in range (|c| 16^2 <= 80,
+// e.g. 2 mm pixels at sigma_z 10: 15) it multiplies rho when rho is read
+// (rho'' = rho 2^(c jc^2)) and a pixel costs one FFMA2 per pixel pair, one ex2
+// per pixel and one FMUL2; otherwise (coarse pixels, where 2^(c jc^2) would
+// underflow while 2^(p' + q' jc) overflows) the full exponent is evaluated,
+// one FADD2 more per pair.  The coefficients p', q' are regenerated on chip for
+// every batch from the event's constants and the row (no per-row coefficient
+// table in memory).
+//
+// Pixel set: exactly the reference's (gaussian_kernel.h:131-137 in its
+// rounding), from the exact per-row intervals of row_table_kernel: an event's
+// row interval [lo, hi) relative to the union start becomes a 32-bit column
+// mask (bit j = column j of the union row), tested once per pixel.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+
+#include "strip_async.cuh"
+#include "strip_device.cuh"
+#include "strip_fast_common.cuh"
+#include "strip_internal.h"
+#include "strip_raster.cuh"
+
+namespace jpet {
+namespace {
+
+constexpr int kURows = 64;       // union rows per batch
+constexpr int kUCols = 32;       // union columns from the even start
+constexpr int kUSW = 4;          // sweeps of 8 columns (4 lanes x 2 pixels)
+constexpr int kUMaxChunk = 512;  // events per chunk
+constexpr int kUMaxE = 8;        // largest batch
+constexpr int kUWinRows = 128;   // window rows the batch former tracks (4 per lane)
+
+// Per-event constants (union_events_kernel): K / K_ref exponent terms as in
+// row_coeff_kernel, and the box relative to the tile's window origin
+// (first row | rows << 8 | first column << 16).
+struct UEvConst {
+  float y, tn, ky, lref;
+  float P, Q, ub;
+  uint32_t box;
+};
+static_assert(sizeof(UEvConst) == 32, "two 16-byte pieces");
+
+// Batch word: first event (offset in the chunk) | events << 10 | union rows << 14
+// | union's first window row << 21.
+__host__ __device__ inline uint32_t ubatch_word(int first, int cnt, int rows, int u0) {
+  return static_cast<uint32_t>(first) | (static_cast<uint32_t>(cnt) << 10) |
+         (static_cast<uint32_t>(rows) << 14) | (static_cast<uint32_t>(u0) << 21);
+}
+__device__ __forceinline__ int ub_first(uint32_t w) { return static_cast<int>(w & 1023u); }
+__device__ __forceinline__ int ub_cnt(uint32_t w) { return static_cast<int>((w >> 10) & 15u); }
+__device__ __forceinline__ int ub_u0(uint32_t w) { return static_cast<int>((w >> 21) & 127u); }
+
+template <int E>
+struct UStage {
+  UEvConst ev[E];
+  uint16_t rows[E][kURows];
+};
+
+template <int E>
+struct USmem {
+  UStage<E> stage[2];
+  float4 pq[2][E][kURows];      // {p, p, q, q} per (event, union row)
+  uint32_t mask[2][E][kURows];  // columns of the union row inside the event's interval
+  uint32_t urow[2][kURows];     // union start column | union width << 16
+  float den_part[2][E][kUMaxE];
+  float gfac[kUCols];           // 2^(c jc^2), jc = j - 16 (split exponent)
+  float cjc[kUCols];            // c jc^2 (full exponent)
+};
+
+template <int E>
+__device__ __forceinline__ void u_issue_stage(UStage<E>& st, const UEvConst* __restrict__ evc,
+                                              const uint16_t* __restrict__ rows, int stride,
+                                              int first, int cnt) {
+  const int tid = threadIdx.x;
+  if (tid < 2 * E) {
+    const int j = tid >> 1, h = tid & 1;
+    const bool v = j < cnt;
+    const int e = first + (v ? j : 0);
+    cp_async16(reinterpret_cast<float4*>(&st.ev[j]) + h,
+               reinterpret_cast<const float4*>(evc + e) + h, v);
+  } else if (tid >= 32 && tid < 32 + E * (kURows / 8)) {
+    const int k = tid - 32;
+    const int j = k >> 3, q = k & 7;
+    const bool v = j < cnt && 8 * q < stride;
+    const size_t src = static_cast<size_t>(first + (v ? j : 0)) * stride + (v ? 8 * q : 0);
+    cp_async16(&st.rows[j][8 * q], rows + src, v);
+  }
+  cp_async_commit();
+}
+
+// Union rows and per-(event, row) records of one batch: NW / 2 threads per
+// union row (consecutive lanes), each handling two events.
+template <int E, int NW>
+__device__ __forceinline__ void u_setup(const DevGeom& g, const FastConst& fc, USmem<E>& S,
+                                        int buf, uint32_t bw, int ox, int oy) {
+  constexpr int kTPR = NW / 2;  // threads per union row
+  static_assert(E == 2 * kTPR, "two events per set-up thread");
+  const UStage<E>& st = S.stage[buf];
+  const int cnt = ub_cnt(bw), u0 = ub_u0(bw);
+  const int r = threadIdx.x / kTPR, sub = threadIdx.x % kTPR;
+  int first[2], width[2];
+  int lo = INT_MAX, hi = INT_MIN;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int j = 2 * sub + k;
+    const uint32_t box = st.ev[j].box;
+    const int ri = u0 + r - static_cast<int>(box & 255u);
+    const bool v = j < cnt && static_cast<unsigned>(ri) < ((box >> 8) & 255u);
+    const uint32_t e = v ? st.rows[j][v ? ri : 0] : 0u;
+    width[k] = static_cast<int>(e >> 8);
+    first[k] = static_cast<int>(box >> 16) + static_cast<int>(e & 255u);
+    if (width[k] > 0) {
+      lo = min(lo, first[k]);
+      hi = max(hi, first[k] + width[k]);
+    }
+  }
+#pragma unroll
+  for (int o = 1; o < kTPR; o <<= 1) {
+    lo = min(lo, __shfl_xor_sync(kFull, lo, o));
+    hi = max(hi, __shfl_xor_sync(kFull, hi, o));
+  }
+  const bool any = lo != INT_MAX;
+  const int u = any ? (lo & ~1) : 0;
+  const int wu = any ? hi - u : 0;
+  if (sub == 0) S.urow[buf][r] = static_cast<uint32_t>(u) | (static_cast<uint32_t>(wu) << 16);
+  const float py = g.tl_y_half_h - static_cast<float>(oy + u0 + r) * g.pixel_height;
+  const float colm = static_cast<float>(ox + u + 16);
+  const float kz2pw = 2.0f * fc.kz * g.pixel_width;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int j = 2 * sub + k;
+    const UEvConst& e = st.ev[j];
+    const float dy = py - e.y;
+    const float lf = e.lref - 0.5f * lg2_approx(fmaf(e.Q, py * py, e.P));
+    const float ua = fmaf(colm, g.pixel_width, e.ub - dy * e.tn);
+    const float p = fmaf(fc.kz * ua, ua, fmaf(e.ky * dy, dy, lf));
+    const float q = kz2pw * ua;
+    const int w = width[k];
+    const int lr = first[k] - u;  // 0 <= lr, lr + w <= wu <= 32
+    const uint32_t bits = (w >= 32) ? 0xFFFFFFFFu : ((1u << w) - 1u);
+    S.pq[buf][j][r] = make_float4(p, p, q, q);
+    S.mask[buf][j][r] = w > 0 ? (bits << lr) : 0u;
+  }
+}
+
+// Forward sums of one row step with SWN active sweeps: rho'' of the owned
+// pixel pairs, then every event's K rho'' (masked to its interval).
+template <int E, int SWN, int RSI, int RS, bool SPLIT>
+__device__ __forceinline__ void u_forward(float2 (&kr)[E][RS][kUSW], float (&dsum)[E],
+                                          const float* w_rho, const USmem<E>& S, int buf, int base,
+                                          int r_u, const float2 (&jc2)[kUSW], int gl) {
+  float2 rr[kUSW], cq[kUSW];
+#pragma unroll
+  for (int s = 0; s < SWN; ++s) {
+    const float2 rv = *reinterpret_cast<const float2*>(w_rho + base + 8 * s);
+    if (SPLIT) {
+      const float2 gv = *reinterpret_cast<const float2*>(&S.gfac[2 * gl + 8 * s]);
+      rr[s] = __fmul2_rn(rv, gv);
+    } else {
+      rr[s] = rv;
+      cq[s] = *reinterpret_cast<const float2*>(&S.cjc[2 * gl + 8 * s]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    const float4 a = S.pq[buf][j][r_u];
+    const uint32_t m = S.mask[buf][j][r_u] >> (2 * gl);
+    const float2 p2 = make_float2(a.x, a.y), q2 = make_float2(a.z, a.w);
+    float2 dd = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int s = 0; s < SWN; ++s) {
+      const float2 e = SPLIT ? __ffma2_rn(q2, jc2[s], p2)
+                             : __ffma2_rn(q2, jc2[s], __fadd2_rn(p2, cq[s]));
+      float2 v = __fmul2_rn(make_float2(ex2_approx(e.x), ex2_approx(e.y)), rr[s]);
+      v.x = (m & (1u << (8 * s))) ? v.x : 0.0f;
+      v.y = (m & (2u << (8 * s))) ? v.y : 0.0f;
+      kr[j][RSI][s] = v;
+      dd = __fadd2_rn(dd, v);
+    }
+    dsum[j] += dd.x + dd.y;
+  }
+}
+
+// Back-projection of one row step: sum_e K_e rho inv_e per owned pixel pair,
+// one read-modify-write of the pair (inside the union row's width).
+template <int E, int SWN, int RSI, int RS>
+__device__ __forceinline__ void u_back(const float2 (&kr)[E][RS][kUSW], const float2 (&inv2)[E],
+                                       float* w_out, int base, int wu, int gl) {
+#pragma unroll
+  for (int s = 0; s < SWN; ++s) {
+    float2 acc = __fmul2_rn(kr[0][RSI][s], inv2[0]);
+#pragma unroll
+    for (int j = 1; j < E; ++j) acc = __ffma2_rn(kr[j][RSI][s], inv2[j], acc);
+    if (2 * gl + 8 * s < wu) {
+      float2* op = reinterpret_cast<float2*>(w_out + base + 8 * s);
+      *op = __fadd2_rn(*op, acc);
+    }
+  }
+}
+
+template <int E, int RSI, int RS, bool SPLIT>
+__device__ __forceinline__ void u_forward_dispatch(int nsw, float2 (&kr)[E][RS][kUSW],
+                                                   float (&dsum)[E], const float* w_rho,
+                                                   const USmem<E>& S, int buf, int base, int r_u,
+                                                   const float2 (&jc2)[kUSW], int gl) {
+  switch (nsw) {
+    case 4: u_forward<E, 4, RSI, RS, SPLIT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 3: u_forward<E, 3, RSI, RS, SPLIT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 2: u_forward<E, 2, RSI, RS, SPLIT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 1: u_forward<E, 1, RSI, RS, SPLIT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    default: break;
+  }
+}
+
+template <int E, int RSI, int RS>
+__device__ __forceinline__ void u_back_dispatch(int nsw, const float2 (&kr)[E][RS][kUSW],
+                                                const float2 (&inv2)[E], float* w_out, int base,
+                                                int wu, int gl) {
+  switch (nsw) {
+    case 4: u_back<E, 4, RSI, RS>(kr, inv2, w_out, base, wu, gl); break;
+    case 3: u_back<E, 3, RSI, RS>(kr, inv2, w_out, base, wu, gl); break;
+    case 2: u_back<E, 2, RSI, RS>(kr, inv2, w_out, base, wu, gl); break;
+    case 1: u_back<E, 1, RSI, RS>(kr, inv2, w_out, base, wu, gl); break;
+    default: break;
+  }
+}
+
+template <int NW>
+constexpr int u_min_blocks() {
+  return NW == 8 ? 2 : 4;
+}
+
+template <int NW, bool SPLIT>
+__global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_kernel(
+    DevGeom g, FastConst fc, Tiling t, const Chunk* __restrict__ chunks,
+    const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
+    const UEvConst* __restrict__ evc, const uint16_t* __restrict__ rows,
+    const uint32_t* __restrict__ batches, const float* __restrict__ rho, float* __restrict__ out,
+    DevCounters* counters) {
+  constexpr int E = NW;                      // events per batch
+  constexpr int kRowsPerStep = NW * 8;       // union rows per step of all warps
+  constexpr int RS = kURows / kRowsPerStep;  // row steps
+  extern __shared__ __align__(16) float smem[];
+  const int pitch = fast_pitch(t);
+  const int wfl = fast_window_floats(t);
+  float* w_rho = smem;
+  float* w_out = smem + wfl;
+  USmem<E>& S = *reinterpret_cast<USmem<E>*>(smem + 2 * wfl);
+
+  const Chunk c = chunks[blockIdx.x];
+  const int ox = c.ox & ~1, oy = c.oy;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gid = lane >> 2, gl = lane & 3;
+  const int nb = c.n_batches;
+  const int stride = t.row_stride;
+  const uint32_t* bws = batches + c.start;
+  auto issue = [&](int b, int buf) {
+    const uint32_t w = bws[b];
+    u_issue_stage<E>(S.stage[buf], evc, rows, stride, c.start + ub_first(w), ub_cnt(w));
+  };
+
+  if (nb > 0) issue(0, 0);
+  if (nb > 1) issue(1, 1);
+  for (int r = warp; r < t.win_h; r += NW) {
+    const int gy = oy + r;
+    for (int col = lane; col < pitch; col += 32) {
+      const int gx = ox + col;
+      w_rho[r * pitch + col] = (gy < g.n_y && gx < g.n_z) ? rho[gy * g.n_z + gx] : 0.0f;
+      w_out[r * pitch + col] = 0.0f;
+    }
+  }
+  for (int i = threadIdx.x; i < 64; i += NW * 32) w_rho[t.win_h * pitch + i] = 0.0f;
+  if (threadIdx.x < kUCols) {
+    const float cz = fc.kz * g.pixel_width * g.pixel_width;
+    const float jc = static_cast<float>(threadIdx.x) - 16.0f;
+    S.cjc[threadIdx.x] = cz * jc * jc;
+    S.gfac[threadIdx.x] = ex2_approx(cz * jc * jc);
+  }
+  float2 jc2[kUSW];
+#pragma unroll
+  for (int s = 0; s < kUSW; ++s) {
+    const float j0 = static_cast<float>(2 * gl + 8 * s) - 16.0f;
+    jc2[s] = make_float2(j0, j0 + 1.0f);
+  }
+  unsigned long long contrib = 0;
+  cp_async_wait_all();
+  __syncthreads();
+  if (nb > 0) u_setup<E, NW>(g, fc, S, 0, bws[0], ox, oy);
+  __syncthreads();
+
+  for (int b = 0; b < nb; ++b) {
+    const int buf = b & 1;
+    const uint32_t bw = bws[b];
+    const int cnt = ub_cnt(bw), u0 = ub_u0(bw);
+    if (b + 2 < nb) issue(b + 2, buf);
+    // ---- forward: this warp's union rows of every event of the batch
+    float2 kr[E][RS][kUSW];
+    float dsum[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) dsum[j] = 0.0f;
+    int base[RS], wu[RS], nsw[RS];
+#pragma unroll
+    for (int rs = 0; rs < RS; ++rs) {
+      const int r_u = kRowsPerStep * rs + 8 * warp + gid;
+      const uint32_t ur = S.urow[buf][r_u];
+      const int wrow = min(u0 + r_u, t.win_h - 1);
+      base[rs] = wrow * pitch + static_cast<int>(ur & 0xFFFFu) + 2 * gl;
+      wu[rs] = static_cast<int>(ur >> 16);
+      nsw[rs] = (__reduce_max_sync(kFull, static_cast<unsigned>(wu[rs])) + 7) >> 3;
+    }
+    u_forward_dispatch<E, 0, RS, SPLIT>(nsw[0], kr, dsum, w_rho, S, buf, base[0], 8 * warp + gid,
+                                        jc2, gl);
+    if (RS > 1)
+      u_forward_dispatch<E, (RS > 1 ? 1 : 0), RS, SPLIT>(nsw[RS - 1], kr, dsum, w_rho, S, buf,
+                                                         base[RS - 1],
+                                                         kRowsPerStep + 8 * warp + gid, jc2, gl);
+    // ---- set-up of the next batch (its staged data was published by the last barrier)
+    if (b + 1 < nb) u_setup<E, NW>(g, fc, S, buf ^ 1, bws[b + 1], ox, oy);
+    {
+      const float tot = rows_transpose_sum<E>(dsum);
+      if (rows_lane_writes<E>(lane)) S.den_part[buf][rows_lane_event<E>(lane)][warp] = tot;
+    }
+    if (b + 2 < nb) cp_async_wait_all();
+    __syncthreads();
+    // ---- denominators: lane j (mod E) adds the warps' partials of event j
+    float inv_l;
+    {
+      const int jl = lane & (E - 1);
+      float den = S.den_part[buf][jl][0];
+#pragma unroll
+      for (int w = 1; w < NW; ++w) den += S.den_part[buf][jl][w];
+      const bool ok = den > 0.0f;  // inv_denominator = 0 otherwise (reconstruction.h:290)
+      inv_l = ok ? __frcp_rn(den) : 0.0f;
+      const unsigned okm = __ballot_sync(kFull, ok && lane < cnt);
+      if (threadIdx.x == 0) contrib += __popc(okm);
+    }
+    float2 inv2[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      const float v = __shfl_sync(kFull, inv_l, j);
+      inv2[j] = make_float2(v, v);
+    }
+    // ---- back-projection into the owned pixel pairs
+    u_back_dispatch<E, 0, RS>(nsw[0], kr, inv2, w_out, base[0], wu[0], gl);
+    if (RS > 1)
+      u_back_dispatch<E, (RS > 1 ? 1 : 0), RS>(nsw[RS - 1], kr, inv2, w_out, base[RS - 1],
+                                               wu[RS - 1], gl);
+  }
+
+  // ---- events outside the batch rectangle: reference-order warp rasteriser
+  __syncthreads();
+  unsigned long long dummy_calls = 0, exact_path = 0;
+  const int nx = c.n_exact;
+  for (int k = warp; k < nx; k += NW) {
+    const int ei = c.start + static_cast<int>(bws[c.count - 1 - k]);
+    WindowAccess acc{w_rho, w_out, ox, oy, pitch};
+    process_event<kCpuReference>(g, 32, ev_geom[ei], ev_box[ei], acc, nullptr, dummy_calls,
+                                 contrib);
+    if (lane == 0) ++exact_path;
+  }
+  if (lane == 0 && contrib) atomicAdd(&counters->n_contributing, contrib);
+  if (lane == 0 && exact_path) atomicAdd(&counters->n_exact_path, exact_path);
+  __syncthreads();
+  for (int r = warp; r < t.win_h; r += NW) {
+    const int gy = oy + r;
+    for (int col = lane; col < pitch; col += 32) {
+      const int gx = ox + col;
+      const float v = w_out[r * pitch + col];
+      if (v != 0.0f && gy < g.n_y && gx < g.n_z) atomicAdd(&out[gy * g.n_z + gx], v);
+    }
+  }
+}
+
+// Per-event constants of the sorted events (the arithmetic of row_coeff_kernel).
+__global__ void union_events_kernel(DevGeom g, FastConst fc, Tiling t, int32_t n,
+                                    const float4* __restrict__ ev_geom,
+                                    const short4* __restrict__ ev_box, UEvConst* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 ev = ev_geom[i];
+  const short4 b = ev_box[i];
+  const float y = ev.y, tn = ev.z, sec = ev.w;
+  const float sec2 = sec * sec;
+  UEvConst c;
+  c.y = y;
+  c.tn = tn;
+  c.ky = fc.kdl * sec2;
+  c.P = fc.two_r2 * sec2 * sec2 * g.ipz;
+  c.Q = 2.0f * sec2 * sec2 * g.ipz + 4.0f * sec2 * tn * tn * g.ipd;
+  c.lref = 0.5f * lg2_approx(fmaf(c.Q, y * y, c.P));
+  c.ub = g.tl_z_half_w - ev.x;
+  const int oy = (b.y / t.tile_h) * t.tile_h;
+  const int ox = ((b.x / t.tile_w) * t.tile_w) & ~1;
+  const int rows = min(b.w - b.y, 255);
+  c.box = static_cast<uint32_t>(b.y - oy) | (static_cast<uint32_t>(rows) << 8) |
+          (static_cast<uint32_t>(b.x - ox) << 16);
+  out[i] = c;
+}
+
+// Greedy batch formation, one warp per chunk: events in sorted order join the
+// current batch while the union stays inside 64 rows x 32 columns and the batch
+// has fewer than max_e events.  Batch words go to batches[c.start ...]; events
+// that fit no batch rectangle alone are listed from the end of the chunk's
+// range (batches[c.start + c.count - 1 - k]).
+__global__ void __launch_bounds__(256) union_batches_kernel(Chunk* __restrict__ chunks,
+                                                            int32_t n_chunks, int32_t max_e,
+                                                            const short4* __restrict__ ev_box,
+                                                            const uint16_t* __restrict__ rows,
+                                                            int32_t stride,
+                                                            uint32_t* __restrict__ batches) {
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_warps = (gridDim.x * blockDim.x) >> 5;
+  for (int ci = wid; ci < n_chunks; ci += n_warps) {
+    const Chunk c = chunks[ci];
+    const int ox = c.ox & ~1, oy = c.oy;
+    int ulo[4], uhi[4];
+    int u0 = INT_MAX, u1 = INT_MIN, cnt = 0, bstart = 0, nb = 0, nx = 0;
+    auto reset = [&]() {
+      cnt = 0;
+      u0 = INT_MAX;
+      u1 = INT_MIN;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        ulo[k] = INT_MAX;
+        uhi[k] = INT_MIN;
+      }
+    };
+    auto emit = [&]() {
+      if (cnt > 0) {
+        if (lane == 0) batches[c.start + nb] = ubatch_word(bstart, cnt, u1 - u0, u0);
+        ++nb;
+      }
+      reset();
+    };
+    reset();
+    for (int i = 0; i < c.count; ++i) {
+      const short4 b = ev_box[c.start + i];
+      const int r0 = b.y - oy, n = b.w - b.y, bx = b.x - ox;
+      const uint16_t* rt = rows + static_cast<size_t>(c.start + i) * stride;
+      int f[4], w[4];
+      bool alone = n <= kURows && r0 >= 0 && r0 + n <= kUWinRows;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int ri = lane + 32 * k - r0;
+        const bool v = ri >= 0 && ri < n && ri < kURows;
+        const uint32_t e = v ? rt[v ? ri : 0] : 0u;
+        w[k] = static_cast<int>(e >> 8);
+        f[k] = bx + static_cast<int>(e & 255u);
+        if (w[k] > 0 && f[k] + w[k] - (f[k] & ~1) > kUCols) alone = false;
+      }
+      alone = __all_sync(kFull, alone);
+      if (!alone) {
+        emit();  // a batch is a contiguous run of events: close the open one first
+        if (lane == 0) batches[c.start + c.count - 1 - nx] = static_cast<uint32_t>(i);
+        ++nx;
+        continue;
+      }
+      // would the event join the current batch?
+      bool join = cnt > 0 && cnt < max_e && max(u1, r0 + n) - min(u0, r0) <= kURows;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (w[k] > 0) {
+          const int lo = min(ulo[k], f[k]), hi = max(uhi[k], f[k] + w[k]);
+          if (hi - (lo & ~1) > kUCols) join = false;
+        }
+      }
+      join = __all_sync(kFull, join);
+      if (!join) {
+        emit();
+        bstart = i;
+      }
+      ++cnt;
+      u0 = min(u0, r0);
+      u1 = max(u1, r0 + n);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (w[k] > 0) {
+          ulo[k] = min(ulo[k], f[k]);
+          uhi[k] = max(uhi[k], f[k] + w[k]);
+        }
+      }
+    }
+    emit();
+    if (lane == 0) {
+      chunks[ci].n_batches = nb;
+      chunks[ci].n_exact = nx;
+    }
+  }
+}
+
+template <int NW>
+size_t u_smem(const Tiling& t) {
+  return 2ull * fast_window_floats(t) * sizeof(float) + sizeof(USmem<NW>);
+}
+
+}  // namespace
+
+size_t union_event_bytes() { return sizeof(UEvConst); }
+
+size_t union_smem_bytes(const Tiling& t) {
+  return t.threads == 256 ? u_smem<8>(t) : u_smem<4>(t);
+}
+
+// whether 2^(c jc^2), |jc| <= 16, may multiply rho (see the file comment)
+bool union_split_exponent(const DevGeom& g, const FastConst& fc) {
+  const float cz = fc.kz * g.pixel_width * g.pixel_width;
+  return -cz * 256.0f <= 80.0f;
+}
+
+cudaError_t union_prepare_kernel(const Tiling& t) {
+  const int bytes = static_cast<int>(union_smem_bytes(t));
+  cudaError_t e;
+  if (t.threads == 256) {
+    e = cudaFuncSetAttribute(iterate_union_kernel<8, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(iterate_union_kernel<8, false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  } else {
+    e = cudaFuncSetAttribute(iterate_union_kernel<4, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(iterate_union_kernel<4, false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  }
+  return e;
+}
+
+cudaError_t launch_union_setup(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                               Chunk* chunks, int32_t n_chunks, int32_t n_events,
+                               const float4* ev_geom, const short4* ev_box, const uint16_t* rows,
+                               void* ev_const, uint32_t* batches, cudaStream_t s) {
+  if (n_events <= 0) return cudaSuccess;
+  if (t.threads != 128 && t.threads != 256) return cudaErrorInvalidValue;
+  union_events_kernel<<<(n_events + 255) / 256, 256, 0, s>>>(
+      g, fc, t, n_events, ev_geom, ev_box, static_cast<UEvConst*>(ev_const));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || n_chunks <= 0) return e;
+  int blocks = (n_chunks + 7) / 8;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  union_batches_kernel<<<blocks, 256, 0, s>>>(chunks, n_chunks, t.threads / 32, ev_box, rows,
+                                              t.row_stride, batches);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
+                                 const short4* ev_box, const void* ev_const,
+                                 const uint16_t* rows, const uint32_t* batches, const float* rho,
+                                 float* out, DevCounters* counters, cudaStream_t s) {
+  if (n_chunks <= 0) return cudaSuccess;
+  if (t.chunk_events > kUMaxChunk || (t.row_stride & 7) != 0 ||
+      (t.threads != 128 && t.threads != 256))
+    return cudaErrorInvalidValue;
+  const bool split = union_split_exponent(g, fc);
+  const auto* evc = static_cast<const UEvConst*>(ev_const);
+  const size_t smem = union_smem_bytes(t);
+  if (t.threads == 256) {
+    auto* k = split ? iterate_union_kernel<8, true> : iterate_union_kernel<8, false>;
+    k<<<n_chunks, 256, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, rows, batches, rho,
+                                  out, counters);
+  } else {
+    auto* k = split ? iterate_union_kernel<4, true> : iterate_union_kernel<4, false>;
+    k<<<n_chunks, 128, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, rows, batches, rho,
+                                  out, counters);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace jpet

@@ -63,8 +63,8 @@ void add_options(Parser& cl) {
   cl.add("rho", 0, "start rho (eg. existing iteration)", Kind::Path, cmd::kOptional, "");
   cl.add_flag("rho-is-int", 0, "start rho uses integer representation (not float)");
   cl.add("kernel", 0,
-         "GPU kernel variant: 0 fast (row-owned), 1 exact (reference operation order), "
-         "2 warp per event",
+         "GPU kernel variant: 0 fast (batch-union), 1 exact (reference operation order), "
+         "2 warp per event, 3 row-owned",
          Kind::Int, cmd::kDontSave, "0");
   cl.add("precision", 0,
          "accumulation: 0 float, 1 compensated tiles, 2 compensated + FP64 denominators, "

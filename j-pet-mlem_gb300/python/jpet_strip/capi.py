@@ -35,6 +35,7 @@ PRECISION_FIXED = 3
 VARIANT_FAST = 0
 VARIANT_EXACT = 1
 VARIANT_WARP = 2
+VARIANT_ROWS = 3
 RASTER_AUTO = 0
 RASTER_SHAPES = {"8x1x1": 1, "8x1x2": 2, "4x1x2": 3, "4x1x3": 4, "4x1x4": 5, "4x2x4": 6,
                  "2x1x6": 7}

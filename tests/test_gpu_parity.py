@@ -13,7 +13,7 @@ from jpet_strip import capi, phantom
 pytestmark = pytest.mark.gpu
 
 TOL_ITER = 1e-5
-VARIANTS = [capi.VARIANT_FAST, capi.VARIANT_EXACT, capi.VARIANT_WARP]
+VARIANTS = [capi.VARIANT_FAST, capi.VARIANT_EXACT, capi.VARIANT_WARP, capi.VARIANT_ROWS]
 
 
 def rel_l2(a, b):
@@ -253,7 +253,7 @@ def test_fast_kernel_register_shapes(sigma):
                                        capi.PRECISION_COMPENSATED, capi.PRECISION_FP64_DEN])
 @pytest.mark.parametrize("shape", sorted(capi.RASTER_SHAPES))
 def test_row_owned_kernel_every_shape(shape, precision, threads):
-    """Every register shape of the default kernel, forced, on 2 mm events whose
+    """Every register shape of the row-owned kernel, forced, on 2 mm events whose
     boxes (64 rows, 22 columns) overflow the small shapes: those events take
     the queued exact path, the rest the register path; both give the
     reference's image and counters."""
@@ -263,7 +263,8 @@ def test_row_owned_kernel_every_shape(shape, precision, threads):
     cg, og = capi.Geometry(*args), O.Geometry(*args)
     want, st = O.mlem_f(og, ev, 1, threads=8)
     with capi.StripReconstruction(cg, precision=precision, block_threads=threads,
-                                  raster_shape=capi.RASTER_SHAPES[shape]) as rec:
+                                  raster_shape=capi.RASTER_SHAPES[shape],
+                                  variant=capi.VARIANT_ROWS) as rec:
         rec.set_events(ev)
         rec.iterate(1)
         got = rec.rho
