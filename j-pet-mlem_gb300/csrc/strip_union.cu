@@ -61,6 +61,12 @@ constexpr int kUSW = 4;          // sweeps of 8 columns (4 lanes x 2 pixels)
 constexpr int kUMaxChunk = 512;  // events per chunk
 constexpr int kUMaxE = 8;        // largest batch
 constexpr int kUWinRows = 128;   // window rows the batch former tracks (4 per lane)
+// Padded per-event strides of the shared-memory batch arrays: the set-up
+// threads of one union row write four different events at once, and with
+// unpadded strides (multiples of 128 bytes) those writes hit the same banks.
+constexpr int kUPqStride = kURows + 1;    // float4 records: events 16 bytes apart in banks
+constexpr int kUMaskStride = kURows + 4;  // 32-bit masks: events 4 banks apart
+constexpr int kUTabStride = kURows + 8;   // 16-bit row entries: events 16 bytes apart
 
 // Per-event constants (union_events_kernel): K / K_ref exponent terms as in
 // row_coeff_kernel, and the box relative to the tile's window origin
@@ -85,14 +91,14 @@ __device__ __forceinline__ int ub_u0(uint32_t w) { return static_cast<int>((w >>
 template <int E>
 struct UStage {
   UEvConst ev[E];
-  uint16_t rows[E][kURows];
+  uint16_t rows[E][kUTabStride];
 };
 
 template <int E>
 struct USmem {
   UStage<E> stage[2];
-  float4 pq[2][E][kURows];      // {p, p, q, q} per (event, union row)
-  uint32_t mask[2][E][kURows];  // columns of the union row inside the event's interval
+  float4 pq[2][E][kUPqStride];      // {p, p, q, q} per (event, union row)
+  uint32_t mask[2][E][kUMaskStride];  // columns of the union row inside the event's interval
   uint32_t urow[2][kURows];     // union start column | union width << 16
   float den_part[2][E][kUMaxE];
   float gfac[kUCols];           // 2^(c jc^2), jc = j - 16 (split exponent)

@@ -91,6 +91,11 @@ WORKLOADS = {
     # full-size plain GPU case: 500 x 450 at 2 mm, 2e7 events, 10 ellipses, 20 iterations
     "plain-2mm-20M": Workload("plain-2mm-20M", 450.0, 1000.0, 450, 500, 2.0, 10.0, 42.0,
                               20_000_000, 20, 2, "random10"),
+    # the full-size case cropped to a quarter of its area with a quarter of its
+    # events (the same event density per pixel, which sets how alike
+    # neighbouring events are): a small case for profiles
+    "plain-2mm-5M-crop": Workload("plain-2mm-5M-crop", 450.0, 1000.0, 225, 250, 2.0, 10.0,
+                                  42.0, 5_000_000, 20, 2, "random10"),
     # precision stress: 1000 x 900 at 1 mm, sigma 5 / 20, lesions at 8x, 1e8 events
     "stress-1mm-100M": Workload("stress-1mm-100M", 450.0, 1000.0, 900, 1000, 1.0, 5.0, 20.0,
                                 100_000_000, 30, 5, "lesions"),
