@@ -37,7 +37,7 @@ extern "C" {
 #define JPET_ERR_CUDA (-2)       /* a CUDA runtime call failed */
 #define JPET_ERR_MEMORY (-3)     /* device or host allocation failed */
 #define JPET_ERR_STATE (-4)      /* call out of order (e.g. iterate before set_events) */
-#define JPET_ERR_TIMEOUT (-5)    /* a bounded device-side wait gave up */
+#define JPET_ERR_TIMEOUT (-5)    /* reserved: no entry point returns it (no device-side waits) */
 #define JPET_ERR_UNSUPPORTED (-6)/* option not built into this library */
 
 typedef struct jpet_strip jpet_strip_t;
@@ -215,15 +215,18 @@ int jpet_strip_nll_grad(jpet_strip_t* h, double sigma_z, double sigma_dl, const 
  * or an application that owns every device allocation and hands out only input
  * and output buffers.  d_responses_aos: device AoS (z_u, z_d, dl) float
  * triples, n <= 1048576 (larger n is rejected with JPET_ERR_ARGUMENT);
- * d_rho_in / d_rho_out: different device float[n_y*n_z] images; the output is
- * cleared by the call.  Work runs on cuda_stream (a cudaStream_t, NULL = the
+ * d_rho_in / d_rho_out: device float[n_y*n_z] images; the output is cleared by
+ * the call, so it may overlap neither the input image nor the responses
+ * (rejected with JPET_ERR_ARGUMENT).  Work runs on cuda_stream (a cudaStream_t, NULL = the
  * default stream) in the reference's CPU float semantics and operation order;
  * no handle is involved.  The per-event working data live in one fixed 24 MiB
  * device array of the library, which every GPU that loads the library keeps
  * until the process exits; calls share it, so calls that overlap on the GPU
  * (different streams or unordered host threads) race, while calls ordered on
- * one stream do not.  The first call on a device looks up the array's address
- * with that device current; make that first call before any stream capture.
+ * one stream do not.  Every call looks up the array's address with the
+ * caller's device current (so a call after cudaDeviceReset is safe); the first
+ * call on a device also loads the library's device code there, so make it
+ * before any stream capture.
  * Errors: jpet_strip_last_error(NULL). */
 int jpet_strip_iterate_noalloc(const jpet_strip_geom* geom, const float* d_responses_aos,
                                int64_t n, const float* d_rho_in, float* d_rho_out,

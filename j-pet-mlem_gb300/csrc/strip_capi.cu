@@ -265,6 +265,14 @@ int fast_width_shape(const DevGeom& g) {
   return w <= 16 ? kShapeS : (w <= 24 ? kShapeM : kShapeL);
 }
 
+// JPET_PRECISION_* -> the fast kernels' accumulation mode
+int precision_code(int precision) {
+  return precision == JPET_PRECISION_COMPENSATED ? kPrecisionCompensated
+         : precision == JPET_PRECISION_FP64_DEN  ? kPrecisionCompensatedDen64
+         : precision == JPET_PRECISION_FIXED     ? kPrecisionFixed
+                                                 : kPrecisionFloat;
+}
+
 int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const float* d_dl,
                    int64_t n, int32_t stride = 1) {
   cudaStream_t s = h->stream;
@@ -401,6 +409,8 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
                                            h->sorted_box.p, h->row_table.p, h->row_pq.p,
                                            h->row_pk.p, h->ev_pk.p, s),
                 "row coefficient launch");
+      JPET_CUDA(h, rows_prepare_kernel(t, precision_code(h->opts.precision)),
+                "row-owned kernel attributes");
     }
     JPET_CUDA(h, cudaMemcpyAsync(&h->table_kernel_calls, h->box_pixels.p,
                                  sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
@@ -725,10 +735,7 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
     if (fixed)
       JPET_CUDA(h, cudaMemsetAsync(h->out64.p, 0, n_pix * sizeof(double), s), "clear image");
     if (h->use_fast) {
-      const int prec = h->opts.precision == JPET_PRECISION_COMPENSATED ? kPrecisionCompensated
-                       : h->opts.precision == JPET_PRECISION_FP64_DEN ? kPrecisionCompensatedDen64
-                       : h->opts.precision == JPET_PRECISION_FIXED    ? kPrecisionFixed
-                                                                      : kPrecisionFloat;
+      const int prec = precision_code(h->opts.precision);
       const uint32_t seed = 0x9E3779B9u * static_cast<uint32_t>(h->iterations_done + 1);
       if (h->use_union) {
         JPET_CUDA(h, launch_iterate_union(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,

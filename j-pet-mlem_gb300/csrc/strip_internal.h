@@ -133,6 +133,9 @@ cudaError_t launch_row_coefficients(const DevGeom& g, const FastConst& fc, const
                                     int32_t n_events, const float4* ev_geom,
                                     const short4* ev_box, const uint16_t* rows, float2* pq,
                                     uint32_t* row_pk, uint32_t* ev_pk, cudaStream_t s);
+// Sets the dynamic shared-memory limit of the row-owned kernel the tiling and
+// precision select (once per event set; launch_iterate_rows only launches).
+cudaError_t rows_prepare_kernel(const Tiling& t, int precision);
 int rows_shape_for(int rows999, int width);
 // rows and columns (2 G SW) an event may span in a register shape
 int rows_shape_rows(int rows_shape);

@@ -14,11 +14,14 @@
 // each, 24 MiB in total) plus the iteration counters; every GPU that loads the
 // library keeps it until the process exits.  All calls share it, so calls
 // whose work overlaps on the GPU (different streams, or different host threads
-// without ordering) race on it; calls ordered on one stream do not.
+// without ordering) race on it; calls ordered on one stream do not.  Each call
+// looks up the array's device address with the caller's device current, so a
+// call after a device reset uses the array of the new context; the first call
+// on a device also loads this library's device code there, so make it before
+// any stream capture.
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 #include <string>
 
 #include "../../include/jpet_strip.h"
@@ -38,10 +41,6 @@ struct NoallocScratch {
 
 static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-NoallocScratch* g_noalloc_ptr[kMaxDevices] = {};
-
 // Per-event set-up (response -> tan, y, z, sec and the clamped box) into the
 // working array; boxes of events that contribute nothing stay as computed and
 // are skipped by the rasteriser (empty rows or columns).
@@ -54,21 +53,24 @@ __global__ void noalloc_prep_kernel(DevGeom g, const float* __restrict__ aos, in
   sc->box[i] = make_short4(e.tl_x, e.tl_y, e.br_x, e.br_y);
 }
 
-// The device address of the working array for the current device; set up on
-// the first call on each device (with that device current).
-NoallocScratch* scratch_for(int device) {
-  if (device < 0 || device >= kMaxDevices) return nullptr;
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) {
-      set_call_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      return nullptr;
-    }
-    g_noalloc_ptr[device] = static_cast<NoallocScratch*>(p);
+// The device address of the working array in the current device's context
+// (looked up on every call: the lookup allocates nothing, and a cached address
+// would dangle after a device reset).
+NoallocScratch* scratch_address() {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) {
+    set_call_error(std::string("jpet_strip_iterate_noalloc: cudaGetSymbolAddress: ") +
+                   cudaGetErrorString(e));
+    return nullptr;
   }
-  return g_noalloc_ptr[device];
+  return static_cast<NoallocScratch*>(p);
+}
+
+// whether the byte ranges [a, a + na) and [b, b + nb) overlap
+bool overlaps(const void* a, size_t na, const void* b, size_t nb) {
+  const uintptr_t pa = reinterpret_cast<uintptr_t>(a), pb = reinterpret_cast<uintptr_t>(b);
+  return na > 0 && nb > 0 && pa < pb + nb && pb < pa + na;
 }
 
 }  // namespace
@@ -95,18 +97,18 @@ int jpet_strip_iterate_noalloc(const jpet_strip_geom* geom, const float* d_respo
     set_call_error("jpet_strip_iterate_noalloc: invalid geometry");
     return JPET_ERR_ARGUMENT;
   }
-  if (d_rho_in == d_rho_out) {
-    set_call_error("jpet_strip_iterate_noalloc: input and output images must differ");
+  const size_t img_bytes =
+      static_cast<size_t>(geom->n_y_pixels) * static_cast<size_t>(geom->n_z_pixels) * sizeof(float);
+  const size_t ev_bytes = static_cast<size_t>(n) * 3 * sizeof(float);
+  // the output is cleared before the inputs are read: it may overlap neither
+  if (overlaps(d_rho_in, img_bytes, d_rho_out, img_bytes) ||
+      overlaps(d_responses_aos, ev_bytes, d_rho_out, img_bytes)) {
+    set_call_error("jpet_strip_iterate_noalloc: the output image overlaps an input buffer");
     return JPET_ERR_ARGUMENT;
   }
-  int device = 0;
-  cudaError_t e = cudaGetDevice(&device);
-  if (e != cudaSuccess) {
-    set_call_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    return JPET_ERR_CUDA;
-  }
-  NoallocScratch* sc = scratch_for(device);
+  NoallocScratch* sc = scratch_address();
   if (!sc) return JPET_ERR_CUDA;
+  cudaError_t e;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   const DevGeom g = make_dev_geom(*geom);
   const size_t n_pix = static_cast<size_t>(g.n_y) * g.n_z;

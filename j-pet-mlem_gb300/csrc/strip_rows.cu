@@ -1,15 +1,15 @@
-// Row-owned MLEM iteration kernel for the CPU-reference semantics (the default
-// fast variant).
+// Row-owned MLEM iteration kernel for the CPU-reference semantics (the ROWS
+// variant; the precision modes and the batched reconstructions run it).
 //
-// One CTA of 8 warps per chunk of events of one image tile, with the rho window
-// and the back-projection window in shared memory, as the other tile kernels.
-// What differs is who writes a window pixel: window row r belongs to warp
-// (r / R) mod 8, R = 32 / G rows per warp step (G lanes per row, two adjacent
-// pixels per lane and sweep), and only that warp ever writes it.  All 8 warps
-// take the same batch of E events: each evaluates its own rows of every event
-// (exp2-form kernel, packed f32x2 math, K rho kept in registers), writes its
-// partial forward sums to shared memory, and after one barrier per batch adds
-// the 8 partials in a fixed order and back-projects K rho / den into its own
+// One CTA of NW warps (4 by default, or 8) per chunk of events of one image
+// tile, with the rho window and the back-projection window in shared memory, as
+// the other tile kernels.  What differs is who writes a window pixel: window row
+// r belongs to warp (r / R) mod NW, R = 32 / G rows per warp step (G lanes per
+// row, two adjacent pixels per lane and sweep), and only that warp ever writes
+// it.  All NW warps take the same batch of E events: each evaluates its own rows
+// of every event (exp2-form kernel, packed f32x2 math, K rho kept in registers),
+// writes its partial forward sums to shared memory, and after one barrier per
+// batch adds the NW partials in a fixed order and back-projects K rho / den into its own
 // rows with plain shared-memory read-modify-write.  No shared-memory atomics
 // are issued (on this GPU a float atomic on shared memory is a load plus a
 // compare-and-swap loop; an integer one is native but still slower than a plain
@@ -254,8 +254,9 @@ __device__ __forceinline__ void rows_chunk(
       // their pass below changes no pixel, so it runs without a branch
       const float inv = __shfl_sync(kFull, inv_l, j);
       // Branch-free read-modify-write of the pixel pair: the pair is always
-      // loaded (inside the window) and stored only if one of its pixels
-      // received a contribution, so no lane writes outside its event's rows.
+      // loaded (inside the window) and stored when its first pixel lies inside
+      // the event's row interval (a zero contribution leaves it unchanged), so
+      // no lane writes outside its event's rows.
       if (ACC == kAccFixed) {
         // q = floor(v 2^22 + U), U uniform in [0, 1) per event: E[q] = v 2^22
         const uint32_t key = hash32(static_cast<uint32_t>(c.start + b * E + j) ^ seed);
@@ -304,9 +305,9 @@ __device__ __forceinline__ void rows_chunk(
                 *reinterpret_cast<float2*>(cp) = cn;
               }
             } else {
-              // one 8-byte store when either pixel received a contribution: the
-              // other pixel of the pair gets o + 0 = o (it lies in the same row,
-              // owned by this warp, inside the window's pitch)
+              // one 8-byte store when the pair's first pixel lies inside the
+              // event's row interval: a pixel without contribution gets o + 0 = o
+              // (the pair lies in one row, owned by this warp, inside the pitch)
               if (2 * gl + kSweep * s < bound[j][rs]) *reinterpret_cast<float2*>(op) = n;
             }
           }
@@ -374,16 +375,16 @@ cudaError_t launch_rows_kernel(const DevGeom& g, const FastConst& fc, const Tili
                                const uint32_t* ev_pk, const uint32_t* rows, const float2* pq,
                                const float* rho,
                                float* out, double* out64, DevCounters* counters, uint32_t seed,
-                               cudaStream_t s) {
+                               cudaStream_t s, int op) {
   constexpr int kPass = NW * (32 / G);
   constexpr int RS = (ROWS + kPass - 1) / kPass;
   constexpr int E = (RS * SW <= 4) ? 8 : (RS * SW <= 8 ? 4 : 2);
   const size_t smem = (ACC == kAccCompensated ? 3ull : 2ull) * fast_window_floats(t) * 4 +
                       2ull * rows_stage_bytes(E, t.row_stride);
   auto* k = iterate_rows_kernel<NW, G, RS, SW, E, ACC, DEN64>;
-  cudaError_t err =
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  if (err != cudaSuccess) return err;
+  if (op == 0)  // once per event set, not per iteration
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(smem));
   k<<<n_chunks, NW * 32, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out,
                                     out64, counters, seed);
   return cudaGetLastError();
@@ -395,24 +396,24 @@ cudaError_t launch_rows_prec(const DevGeom& g, const FastConst& fc, const Tiling
                              const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
                               const float2* pq,
                              const float* rho, float* out, double* out64, DevCounters* counters,
-                             int precision, uint32_t seed, cudaStream_t s) {
+                             int precision, uint32_t seed, cudaStream_t s, int op) {
   switch (precision) {
     case kPrecisionCompensated:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccCompensated, false>(
           g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
-          s);
+          s, op);
     case kPrecisionCompensatedDen64:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccCompensated, true>(
           g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
-          s);
+          s, op);
     case kPrecisionFixed:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccFixed, false>(
           g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
-          s);
+          s, op);
     default:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccFloat, false>(
           g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
-          s);
+          s, op);
   }
 }
 
@@ -424,12 +425,12 @@ cudaError_t launch_rows_shape(const DevGeom& g, const FastConst& fc, const Tilin
                               const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
                               const float2* pq,
                               const float* rho, float* out, double* out64, DevCounters* counters,
-                              int precision, uint32_t seed, cudaStream_t s) {
+                              int precision, uint32_t seed, cudaStream_t s, int op) {
   if (t.threads == 256)
     return launch_rows_prec<8, G, ROWS, SW>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq,
-                                            rho, out, out64, counters, precision, seed, s);
+                                            rho, out, out64, counters, precision, seed, s, op);
   return launch_rows_prec<4, G, ROWS, SW>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq,
-                                          rho, out, out64, counters, precision, seed, s);
+                                          rho, out, out64, counters, precision, seed, s, op);
 }
 
 // ---- batched reconstructions ------------------------------------------------------
@@ -558,38 +559,53 @@ int rows_shape_for(int rows999, int width) {
   return kRowsShape4x2x4;
 }
 
-cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Tiling& t,
+static cudaError_t rows_dispatch(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
                               const float2* pq,
                                 const float* rho, float* out, double* out64,
                                 DevCounters* counters, int precision, uint32_t seed,
-                                cudaStream_t s) {
-  if (n_chunks <= 0) return cudaSuccess;
+                                cudaStream_t s, int op) {
+  if (op != 0 && n_chunks <= 0) return cudaSuccess;
   if (t.chunk_events > kMaxChunkEvents || (t.row_stride & 7) != 0) return cudaErrorInvalidValue;
   switch (t.rows_shape) {
     case kRowsShape8x1x1:
       return launch_rows_shape<8, 32, 1>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s);
+                                         out, out64, counters, precision, seed, s, op);
     case kRowsShape8x1x2:
       return launch_rows_shape<8, 32, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s);
+                                         out, out64, counters, precision, seed, s, op);
     case kRowsShape4x1x2:
       return launch_rows_shape<4, 64, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s);
+                                         out, out64, counters, precision, seed, s, op);
     case kRowsShape4x1x3:
       return launch_rows_shape<4, 64, 3>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s);
+                                         out, out64, counters, precision, seed, s, op);
     case kRowsShape4x1x4:
       return launch_rows_shape<4, 64, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s);
+                                         out, out64, counters, precision, seed, s, op);
     case kRowsShape2x1x6:
       return launch_rows_shape<2, 64, 6>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s);
+                                         out, out64, counters, precision, seed, s, op);
     default:
       return launch_rows_shape<4, 128, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                          out, out64, counters, precision, seed, s);
+                                          out, out64, counters, precision, seed, s, op);
   }
+}
+
+cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Tiling& t,
+                                const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
+                                const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
+                                const float2* pq, const float* rho, float* out, double* out64,
+                                DevCounters* counters, int precision, uint32_t seed,
+                                cudaStream_t s) {
+  return rows_dispatch(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out,
+                       out64, counters, precision, seed, s, 1);
+}
+
+cudaError_t rows_prepare_kernel(const Tiling& t, int precision) {
+  return rows_dispatch(DevGeom{}, FastConst{}, t, nullptr, 0, nullptr, nullptr, nullptr, nullptr,
+                       nullptr, nullptr, nullptr, nullptr, nullptr, precision, 0u, nullptr, 0);
 }
 
 size_t rows_smem_bytes(const Tiling& t, int threads, int rows_shape) {

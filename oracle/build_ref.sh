@@ -19,10 +19,16 @@
 #               CMakeLists.txt:19 sets it.
 #
 # The reference's CMake project is not used (it does not configure with CMake 4).
-# Sources are read in place from $JPET_REFERENCE (default /root/reference); nothing
-# is copied.  When the sources are absent the script exits 0 and builds nothing.
+# Sources are read in place from the reference checkout named by $JPET_REFERENCE
+# (required; the build entry point sets it where the checkout exists); nothing is
+# copied.  When the variable is unset or the sources are absent the script exits
+# 0 and builds nothing.
 set -e
-REF=${JPET_REFERENCE:-/root/reference}
+REF=${JPET_REFERENCE:-}
+if [ -z "$REF" ]; then
+  echo "build_ref: JPET_REFERENCE is not set; skipping" >&2
+  exit 0
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/src/2d/strip/reconstruction_cmd.cpp" ]; then

@@ -45,6 +45,15 @@ def test_noalloc_matches_handle_entry_point(golden):
             got = dst.cpu().numpy()
             assert rel_l2(got, want) < TOL_ITER, (call, rel_l2(got, want))
             src, dst = dst, src
+    # a warm call allocates no device memory: free memory is the same before and after
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    rc = L.jpet_strip_iterate_noalloc(C.byref(cg), ev_d.data_ptr(), len(ev), src.data_ptr(),
+                                      dst.data_ptr(), stream)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert rc == capi.JPET_OK
+    assert free1 == free0, (free0, free1)
 
 
 def test_noalloc_rejects_oversized_and_bad_arguments():
@@ -59,5 +68,13 @@ def test_noalloc_rejects_oversized_and_bad_arguments():
     assert rc == capi.JPET_ERR_ARGUMENT
     assert b"at most 1048576" in L.jpet_strip_last_error(None)
     rc = L.jpet_strip_iterate_noalloc(C.byref(cg), ev.data_ptr(), 4, a.data_ptr(), a.data_ptr(),
+                                      None)
+    assert rc == capi.JPET_ERR_ARGUMENT
+    # partly overlapping images, and an output over the responses
+    rc = L.jpet_strip_iterate_noalloc(C.byref(cg), ev.data_ptr(), 4, a.data_ptr(),
+                                      a.data_ptr() + 4 * 100, None)
+    assert rc == capi.JPET_ERR_ARGUMENT
+    assert b"overlaps" in L.jpet_strip_last_error(None)
+    rc = L.jpet_strip_iterate_noalloc(C.byref(cg), a.data_ptr(), 4, b.data_ptr(), a.data_ptr(),
                                       None)
     assert rc == capi.JPET_ERR_ARGUMENT
