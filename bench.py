@@ -61,6 +61,14 @@ def parse():
                    help="skip the differentiable form (adjoint throughput and calibration)")
     p.add_argument("--sample-events", type=int, default=1_000_000,
                    help="events of the FP64-oracle prefix in the precision report")
+    p.add_argument("--no-accuracy", action="store_true",
+                   help="skip the accuracy entry (stated configurations vs the oracles)")
+    p.add_argument("--no-precision", action="store_true",
+                   help="skip the precision entry (every accumulation mode vs FP64)")
+    p.add_argument("--accuracy-events", type=int, default=2_000_000,
+                   help="events of the prefix iterated against the reference float path")
+    p.add_argument("--accuracy-report", action="store_true",
+                   help="every iteration of the full workload against the FP64 GPU iteration")
     p.add_argument("--precision-report", action="store_true",
                    help="print the precision-stress comparison instead of the headline line")
     p.add_argument("--variant", type=int, default=0,
@@ -73,6 +81,15 @@ def parse():
                    help="0 FP32 tile sums, 1 compensated tile sums, 2 plus FP64 denominators, "
                         "3 fixed-point tile sums")
     return p.parse_args()
+
+
+def config_of(wl, n_events, world):
+    """The workload description both arms print."""
+    return {"workload": wl.name, "events": n_events, "grid": f"{wl.n_z}x{wl.n_y}",
+            "pixel_mm": wl.pixel, "sigma_z": wl.sigma_z, "sigma_dl": wl.sigma_dl,
+            "phantom": wl.phantom, "seed": wl.seed,
+            "l2": "inputs larger than L2 (prepared events and row tables, ~160 B each)",
+            "parallelism": f"replicas{world}"}
 
 
 def replica_value(local_ms, n_events, steps, world, device="cpu"):
@@ -176,11 +193,11 @@ def cpu_sample_rate(wl, events, budget_s: float, threads: int):
     og = oracle.Geometry(*wl.geometry_args())
     probe = min(len(events), 20000)
     t = time.perf_counter()
-    oracle.mlem_f(og, events[:probe], 1, threads=threads)
+    oracle.mlem_f(og, events[:probe], 1, threads=threads, release=True)
     dt = max(time.perf_counter() - t, 1e-3)
     n = int(min(len(events), max(probe, probe * budget_s / dt)))
     t = time.perf_counter()
-    _, st = oracle.mlem_f(og, events[:n], 1, threads=threads)
+    _, st = oracle.mlem_f(og, events[:n], 1, threads=threads, release=True)
     dt = time.perf_counter() - t
     return n, dt, st
 
@@ -192,25 +209,35 @@ def reference_arm(args, wl, world, rank):
 
     threads = os.cpu_count() or 1
     n_all = args.events or wl.n_events
-    # sample sized so that each step is a few seconds of the CPU path
+    # the events the GPU arm iterates (the same generator, seed and count; the
+    # seeded CPU generator where no GPU is present), then a prefix sized so
+    # that each step is a few seconds of the CPU path
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
-    probe_ev = wl.events(min(n_all, 20000), device=None)
+    try:
+        import torch
+
+        gpu = torch.cuda.is_available()
+    except ImportError:
+        gpu = False
+    all_ev = wl.events(n_all, device=0 if gpu else None)
     og = oracle.Geometry(*wl.geometry_args())
+    probe_ev = all_ev[:min(n_all, 20000)]
     t = time.perf_counter()
-    oracle.mlem_f(og, probe_ev, 1, threads=threads)
+    oracle.mlem_f(og, probe_ev, 1, threads=threads, release=True)
     rate = len(probe_ev) / max(time.perf_counter() - t, 1e-3)
     budget = max(2.0, 120.0 / max(1, args.steps + args.warmup))
     n = int(min(n_all, max(len(probe_ev), rate * budget)))
-    ev = wl.events(n, device=None)
+    ev = np.ascontiguousarray(all_ev[:n])
+    del all_ev
     rho = None
     for _ in range(args.warmup):
-        rho, _ = oracle.mlem_f(og, ev, 1, rho, threads=threads)
+        rho, _ = oracle.mlem_f(og, ev, 1, rho, threads=threads, release=True)
     times = []
     for _ in range(args.steps):
         t = time.perf_counter()
-        rho, st = oracle.mlem_f(og, ev, 1, rho, threads=threads)
+        rho, st = oracle.mlem_f(og, ev, 1, rho, threads=threads, release=True)
         times.append(time.perf_counter() - t)
     total = sum(times)
     value = n * args.steps / total
@@ -220,11 +247,13 @@ def reference_arm(args, wl, world, rank):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wl.name, "events": n_all, "grid": f"{wl.n_z}x{wl.n_y}",
-                   "pixel_mm": wl.pixel, "sigma_z": wl.sigma_z, "sigma_dl": wl.sigma_dl},
+        "config": config_of(wl, n_all, world),
         "kernel_pixel_evals_per_s": evals * args.steps / total,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"first {n} of {n_all} events, one iteration per step"},
+                         "build": "oracle/liboracle_strip_release.so (-O3, OpenMP, FMA contraction)",
+                         "sample": f"first {n} of the {n_all} events the GPU arm iterates "
+                                   f"({'GPU' if gpu else 'CPU'} generator, seed {wl.seed}), "
+                                   f"one iteration per step"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -275,36 +304,24 @@ def gb300_arm(args, wl, world, rank, local):
     kernel_ms = statistics.mean(per_step_ms)
     evals_per_s = evals_per_iter / (kernel_ms * 1e-3)
 
-    # accuracy on a sample: one iteration vs the float and FP64 oracles
+    # accuracy at the stated configurations, and the CPU baseline
     accuracy = None
     cpu = None
+    precision = None
+    kopts = dict(variant=args.variant, precision=args.precision, raster_shape=args.raster_shape,
+                 block_threads=args.block_threads)
     if rank == 0:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle
-
-        og = oracle.Geometry(*wl.geometry_args())
-        sample = events[:200000]
-        with capi.StripReconstruction(geom, device=local, variant=args.variant,
-                                      precision=args.precision,
-                                      raster_shape=args.raster_shape,
-                                      block_threads=args.block_threads) as r2:
-            r2.set_events(sample)
-            r2.iterate(1)
-            got = r2.rho.astype(np.float64)
-        f32, _ = oracle.mlem_f(og, sample, 1, threads=os.cpu_count() or 1)
-        f64 = oracle.mlem_d(og, sample, 1, threads=os.cpu_count() or 1)
-        accuracy = {
-            "sample_events": len(sample), "iterations": 1,
-            "rel_l2_vs_reference_float": float(np.linalg.norm(got - f32) / np.linalg.norm(f32)),
-            "rel_l2_vs_fp64": float(np.linalg.norm(got - f64) / np.linalg.norm(f64)),
-            "reference_float_rel_l2_vs_fp64": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
-            "tolerance": 1e-5,
-        }
+        if not args.no_accuracy:
+            accuracy = accuracy_report(args, wl, geom, events, local, kopts)
+        if not args.no_precision:
+            precision = precision_modes(wl, geom, events, local)
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             n, dt, st = cpu_sample_rate(wl, events, args.cpu_seconds, threads)
             cpu = {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": f"first {n} of {n_events} events, one iteration from a uniform image",
+                   "build": "oracle/liboracle_strip_release.so (-O3, OpenMP, FMA contraction)",
+                   "sample": f"first {n} of the {n_events} events the GPU arm iterates, "
+                             f"one iteration from a uniform image",
                    "kernel_pixel_evals_per_s": st["n_kernel_calls"] / dt}
 
     # end to end through the C ABI with host buffers (pinned)
@@ -346,9 +363,10 @@ def gb300_arm(args, wl, world, rank, local):
     if peaks:
         ex2_peak = peaks["ex2_per_s"]
         atom_peak = peaks["shared_atomic_per_s"]
-        if args.variant == 0:
-            # row-owned kernel: one exp per kernel-pixel evaluation and no
-            # shared-memory atomics (plain read-modify-write of owned rows)
+        if args.variant in (0, 3):
+            # batch-union and row-owned kernels: one exp per kernel-pixel
+            # evaluation and no shared-memory atomics (plain read-modify-write
+            # of owned pixels)
             bound_sfu = True
         else:
             # one exp and one shared-memory float atomic per evaluation: the
@@ -361,13 +379,13 @@ def gb300_arm(args, wl, world, rank, local):
                     "frac": evals_per_s / peak,
                     "peak_source": "measured on this GPU by libjpet_peaks (ex2.approx and "
                                    "shared float atomicAdd throughput)",
-                    "traffic": profile_traffic(n_events),
+                    "traffic": profile_traffic(n_events, variant=args.variant),
                     "sfu_frac": evals_per_s / ex2_peak,
                     "shared_atomic_frac": evals_per_s / atom_peak,
                     "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_kind}
-        if args.variant == 0:
-            traffic = profile_traffic(n_events)
-            insts = profile_traffic(n_events, "warp_instructions_per_launch")
+        if args.variant in (0, 3):
+            traffic = profile_traffic(n_events, variant=args.variant)
+            insts = profile_traffic(n_events, "warp_instructions_per_launch", args.variant)
             if traffic:
                 roofline["hbm_achieved_gbs"] = traffic / (kernel_ms * 1e-3) / 1e9
                 roofline["hbm_frac"] = roofline["hbm_achieved_gbs"] / hbm
@@ -388,15 +406,12 @@ def gb300_arm(args, wl, world, rank, local):
                    "precision": ["fp32", "compensated", "fp64_den", "fixed"][args.precision]},
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wl.name, "events": n_events, "grid": f"{wl.n_z}x{wl.n_y}",
-                   "pixel_mm": wl.pixel, "sigma_z": wl.sigma_z, "sigma_dl": wl.sigma_dl,
-                   "phantom": wl.phantom, "seed": wl.seed,
-                   "l2": "inputs larger than L2 (prepared events 24 B each)",
-                   "parallelism": f"replicas{world}"},
+        "config": config_of(wl, n_events, world),
         "kernel_pixel_evals_per_s": world * evals_per_s,
         "evals_per_event": evals_per_iter / n_events,
         "roofline": roofline,
         "accuracy": accuracy,
+        "precision": precision,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(12 * n_events + 4 * wl.n_y * wl.n_z),
@@ -413,12 +428,197 @@ def gb300_arm(args, wl, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
-def profile_traffic(n_events, key="dram_bytes_per_launch"):
+def _rel(a, b):
+    import numpy as np
+
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def accuracy_report(args, wl, geom, events, local, kopts):
+    """Accuracy at the stated configurations (tolerance 1e-5 relative L2 per
+    iteration against the reference float path, 1e-4 after 20 iterations):
+      prefix   the first accuracy-events (2e6) of this workload's events, every
+               iteration of the workload (20): each GPU iteration started from
+               the reference float path's previous image (single-step error),
+               the free-running GPU iterations against the free-running
+               reference float path, and both against the reference iteration
+               at double (jpet_strip_reference_fp64, free-running; rel L2 and
+               max-abs per iteration);
+      full     every event, one iteration against that FP64 iteration (the
+               20-iteration full-size comparison is bench.py --accuracy-report:
+               at 2e7 events the FP64 iteration takes ~9 s);
+      config1  the CPU-runnable case exactly: 200 x 180 at 5 mm, 1e6 events of
+               the 3-ellipse phantom, 10 free-running iterations against the
+               reference float path (and the FP64 oracle at the end)."""
+    import concurrent.futures as cf
+
+    import numpy as np
+    import torch
+
+    from jpet_strip import capi
+    from jpet_strip.workloads import WORKLOADS
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    threads = os.cpu_count() or 1
+    og = oracle.Geometry(*wl.geometry_args())
+    iters = wl.iterations
+    m = min(len(events), args.accuracy_events)
+    pre = np.ascontiguousarray(events[:m])
+
+    def oracle_chain(geom_o, ev, n_iter):
+        out, rho = [], None
+        for _ in range(n_iter):
+            rho, _ = oracle.mlem_f(geom_o, ev, 1, rho, threads=threads)
+            out.append(rho)
+        return out
+
+    pool = cf.ThreadPoolExecutor(max_workers=1)  # the CPU chain overlaps the GPU work
+    fut = pool.submit(oracle_chain, og, pre, iters)
+    pre_d = torch.from_numpy(pre).cuda(local)
+    free_imgs, f64_imgs, f64 = [], [], None
+    with capi.StripReconstruction(geom, device=local, **kopts) as r:
+        r.set_events(pre)
+        for _ in range(iters):
+            r.iterate(1)
+            free_imgs.append(r.rho)
+    for _ in range(iters):
+        f64, _ = capi.reference_fp64(geom, pre_d, 1, rho=f64, device=local)
+        f64_imgs.append(f64)
+    ref = fut.result()
+    single = []
+    with capi.StripReconstruction(geom, device=local, **kopts) as r:
+        r.set_events(pre)
+        for it in range(iters):
+            if it > 0:
+                r.rho = ref[it - 1]
+            r.iterate(1)
+            single.append(_rel(r.rho, ref[it]))
+    prefix = {
+        "events": m, "iterations": iters,
+        "single_step_rel_l2_vs_reference_float": single,
+        "free_rel_l2_vs_reference_float": [_rel(a, b) for a, b in zip(free_imgs, ref)],
+        "free_rel_l2_vs_fp64": [_rel(a, b) for a, b in zip(free_imgs, f64_imgs)],
+        "free_max_abs_vs_fp64": [float(np.abs(a - b).max()) for a, b in zip(free_imgs, f64_imgs)],
+        "reference_float_rel_l2_vs_fp64": [_rel(a, b) for a, b in zip(ref, f64_imgs)],
+        "reference_float_max_abs_vs_fp64": [float(np.abs(a - b).max())
+                                            for a, b in zip(ref, f64_imgs)],
+    }
+    prefix["within_tolerance"] = bool(max(single) <= 1e-5 and
+                                      prefix["free_rel_l2_vs_reference_float"][-1] <= 1e-4)
+    # full size, one iteration against FP64
+    ev_d = torch.from_numpy(np.ascontiguousarray(events)).cuda(local)
+    t0 = time.perf_counter()
+    f64_full, _ = capi.reference_fp64(geom, ev_d, 1, device=local)
+    fp64_s = time.perf_counter() - t0
+    with capi.StripReconstruction(geom, device=local, **kopts) as r:
+        r.set_events(events)
+        r.iterate(1)
+        got = r.rho
+    del ev_d
+    full = {"events": len(events), "iterations": 1, "rel_l2_vs_fp64": _rel(got, f64_full),
+            "max_abs_vs_fp64": float(np.abs(got - f64_full).max()),
+            "fp64_seconds_per_iteration": fp64_s}
+    # config 1 exactly as stated
+    w1 = WORKLOADS["plain-5mm-1M"]
+    g1 = capi.Geometry(*w1.geometry_args())
+    o1 = oracle.Geometry(*w1.geometry_args())
+    ev1 = w1.events(w1.n_events, device=local)
+    ref1 = oracle_chain(o1, ev1, w1.iterations)
+    d1 = oracle.mlem_d(o1, ev1, w1.iterations, threads=threads)
+    imgs1 = []
+    with capi.StripReconstruction(g1, device=local, **kopts) as r:
+        r.set_events(ev1)
+        for _ in range(w1.iterations):
+            r.iterate(1)
+            imgs1.append(r.rho)
+    config1 = {"workload": w1.name, "events": len(ev1), "iterations": w1.iterations,
+               "free_rel_l2_vs_reference_float": [_rel(a, b) for a, b in zip(imgs1, ref1)],
+               "final_rel_l2_vs_fp64": _rel(imgs1[-1], d1),
+               "reference_float_final_rel_l2_vs_fp64": _rel(ref1[-1], d1)}
+    pool.shutdown()
+    return {"tolerance_per_iteration": 1e-5, "tolerance_20_iterations": 1e-4,
+            "config2_prefix": prefix, "config2_full": full, "config1": config1}
+
+
+def precision_modes(wl, geom, events, local):
+    """Every accumulation mode on this workload: ms per iteration (CUDA events,
+    3 iterations after a warm-up) and, after one iteration from a uniform image,
+    rel L2 and max-abs against the reference iteration at double on the GPU."""
+    import numpy as np
+    import torch
+
+    from jpet_strip import capi
+
+    ev_d = torch.from_numpy(np.ascontiguousarray(events)).cuda(local)
+    f64, _ = capi.reference_fp64(geom, ev_d, 1, device=local)
+    del ev_d
+    out = {"events": len(events), "reference": "jpet_strip_reference_fp64, one iteration"}
+    modes = [("fp32", capi.PRECISION_FP32), ("compensated", capi.PRECISION_COMPENSATED),
+             ("compensated_fp64_den", capi.PRECISION_FP64_DEN), ("fixed", capi.PRECISION_FIXED)]
+    stream = torch.cuda.Stream(device=local)
+    for name, prec in modes:
+        with capi.StripReconstruction(geom, device=local, precision=prec) as r:
+            r.set_stream(stream.cuda_stream)
+            r.set_events(events)
+            r.iterate(1)
+            img = r.rho
+            r.iterate(1)  # warm-up
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            r.synchronize()
+            a.record(stream)
+            r.iterate(3)
+            b.record(stream)
+            b.synchronize()
+            out[name] = {"ms_per_iteration": a.elapsed_time(b) / 3,
+                         "rel_l2_vs_fp64": _rel(img, f64),
+                         "max_abs_vs_fp64": float(np.abs(img - f64).max())}
+    return out
+
+
+def accuracy_full_report(args, wl, local):
+    """bench.py --accuracy-report: every iteration of the full workload, the
+    default FP32 kernel against the reference iteration at double on the GPU
+    (both free-running from a uniform image): rel L2 and max-abs per iteration."""
+    import numpy as np
+    import torch
+
+    from jpet_strip import capi
+
+    n = args.events or wl.n_events
+    events = wl.events(n, device=local)
+    geom = capi.Geometry(*wl.geometry_args())
+    ev_d = torch.from_numpy(np.ascontiguousarray(events)).cuda(local)
+    rel, mx = [], []
+    f64 = None
+    with capi.StripReconstruction(geom, device=local) as r:
+        r.set_events(events)
+        for _ in range(wl.iterations):
+            r.iterate(1)
+            f64, _ = capi.reference_fp64(geom, ev_d, 1, rho=f64, device=local)
+            got = r.rho
+            rel.append(_rel(got, f64))
+            mx.append(float(np.abs(got - f64).max()))
+    print(json.dumps({"metric": "per-iteration accuracy of the FP32 iteration vs FP64",
+                      "config": {"workload": wl.name, "events": n, "iterations": wl.iterations},
+                      "rel_l2_vs_fp64": rel, "max_abs_vs_fp64": mx}), flush=True)
+
+
+
+def profile_traffic(n_events, key="dram_bytes_per_launch", variant=0):
     """DRAM bytes (or warp instructions, key "warp_instructions_per_launch") per
-    iteration-kernel launch from the committed ncu summary of the row-owned
-    kernel (dram__bytes_read.sum + dram__bytes_write.sum, smsp__inst_executed.sum
-    of one captured launch), scaled from the captured event count to n_events."""
-    path = os.path.join(ROOT, "profiles", "iterate_rows_traffic.json")
+    iteration-kernel launch from the committed ncu capture of the kernel the
+    variant runs (dram__bytes_read.sum + dram__bytes_write.sum,
+    smsp__inst_executed.sum of one launch), scaled from the captured event count
+    to n_events."""
+    name = {0: "iterate_union_traffic.json", 3: "iterate_rows_traffic.json"}.get(variant)
+    if name is None:
+        return None
+    path = os.path.join(ROOT, "profiles", name)
     try:
         with open(path) as f:
             d = json.load(f)
@@ -645,6 +845,8 @@ def main():
         reference_arm(args, wl, world, rank)
     elif args.precision_report:
         precision_report(args, local)
+    elif args.accuracy_report:
+        accuracy_full_report(args, wl, local)
     else:
         gb300_arm(args, wl, world, rank, local)
 

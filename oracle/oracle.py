@@ -14,6 +14,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle_strip.so")
+# the same restatement built with FP contraction allowed: the CPU baseline's timing build
+RELEASE_LIB_PATH = os.path.join(HERE, "liboracle_strip_release.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 
@@ -62,15 +64,17 @@ def build() -> str:
     return LIB_PATH
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH):
+def lib(release: bool = False):
+    """The parity oracle, or with release=True its timing build (FMA contraction
+    allowed, so results differ from the strict one by rounding)."""
+    path = RELEASE_LIB_PATH if release else LIB_PATH
+    if path not in _libs:
+        if not os.path.exists(path):
             build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(path)
         f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
         f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
         gp = C.POINTER(OrcGeom)
@@ -110,8 +114,8 @@ def lib():
         L.orc_event_box_f.argtypes = [gp, C.c_float, C.c_float, C.c_float] + [C.POINTER(C.c_int32)] * 4
         L.orc_event_box_f.restype = C.c_int32
         L.orc_to_projection_space_tan_d.argtypes = [C.c_double] * 4 + [C.POINTER(C.c_double)] * 3
-        _lib = L
-    return _lib
+        _libs[path] = L
+    return _libs[path]
 
 
 def _events(ev) -> np.ndarray:
@@ -119,15 +123,17 @@ def _events(ev) -> np.ndarray:
     return ev
 
 
-def mlem_f(geom: Geometry, events, n_iterations: int, rho=None, threads: int = 1):
-    """Reference CPU float path: returns (rho float32[n_y, n_z], stats dict)."""
+def mlem_f(geom: Geometry, events, n_iterations: int, rho=None, threads: int = 1,
+           release: bool = False):
+    """Reference CPU float path: returns (rho float32[n_y, n_z], stats dict).
+    release=True runs the timing build (FMA contraction allowed)."""
     ev = _events(events)
     r = (np.ones(geom.n_y * geom.n_z, np.float32) if rho is None
          else np.ascontiguousarray(rho, np.float32).reshape(-1).copy())
     st = OrcStats()
     g = geom.c()
-    rc = lib().orc_mlem_f(C.byref(g), ev.reshape(-1), len(ev), r, n_iterations, threads,
-                          C.byref(st))
+    rc = lib(release).orc_mlem_f(C.byref(g), ev.reshape(-1), len(ev), r, n_iterations, threads,
+                                 C.byref(st))
     if rc != 0:
         raise RuntimeError("orc_mlem_f failed")
     return r.reshape(geom.n_y, geom.n_z), dict(
