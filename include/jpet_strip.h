@@ -66,13 +66,16 @@ typedef struct jpet_strip_geom {
 #define JPET_PRECISION_FP32 0        /* FP32 evaluation, FP32 shared-memory tile sums, FP32 image */
 #define JPET_PRECISION_COMPENSATED 1 /* FP32 evaluation; every shared-memory tile addition
                                         also adds its exact rounding error (TwoSum) to a
-                                        compensation tile; tile sum + compensation go into
-                                        an FP64 image (compensated, Kahan-style, per tile) */
+                                        compensation tile; tiles go into an FP32 image whose
+                                        atomic additions' rounding errors (TwoSum of the value
+                                        each atomic found), with the tile compensations, go
+                                        into an FP32 compensation image added at the end */
 #define JPET_PRECISION_FP64_DEN 2    /* as COMPENSATED, plus per-event denominators reduced
-                                        in FP64 */
-#define JPET_PRECISION_FIXED 3       /* deterministic tiles: each contribution rounded once to
-                                        2^-22 of an event (unbiased per-event dither) and
-                                        summed with integer shared atomics; FP64 image */
+                                        in FP64 (the only FP64 arithmetic of the modes) */
+#define JPET_PRECISION_FIXED 3       /* deterministic image: each contribution rounded once to
+                                        2^-22 of an event (unbiased per-event dither), summed
+                                        with integer shared atomics per tile and 64-bit integer
+                                        atomics over tiles, converted to FP32 once */
 
 /* iteration kernel */
 #define JPET_VARIANT_FAST 0  /* default.  FP32: batch-union kernel -- batches of <= 8 similar

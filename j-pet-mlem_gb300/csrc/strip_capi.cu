@@ -69,7 +69,8 @@ struct jpet_strip {
   std::string last_error = "no error";
 
   DevBuf<float> rho, out, sens_point, sens_pixel;
-  DevBuf<double> out64;              // FP64 image of the compensated modes
+  DevBuf<float> out_lo;              // compensation image of the compensated modes
+  DevBuf<unsigned long long> out_q;  // 64-bit fixed-point image of the FIXED mode
   DevBuf<float> raw;                 // staging for uploaded events (kept for the next upload)
   DevBuf<float4> ev_geom, sorted_geom, over_geom;
   DevBuf<short4> ev_box, sorted_box, over_box;
@@ -601,7 +602,10 @@ int jpet_strip_create(const jpet_strip_geom* geom, const jpet_strip_opts* opts,
   }
   h->stream = h->own_stream;
   const size_t n_pix = static_cast<size_t>(h->g.n_y) * h->g.n_z;
-  if ((o.precision != JPET_PRECISION_FP32 && h->out64.alloc(n_pix) != cudaSuccess) ||
+  const bool comp = o.precision == JPET_PRECISION_COMPENSATED ||
+                    o.precision == JPET_PRECISION_FP64_DEN;
+  if ((comp && h->out_lo.alloc(n_pix) != cudaSuccess) ||
+      (o.precision == JPET_PRECISION_FIXED && h->out_q.alloc(n_pix) != cudaSuccess) ||
       h->rho.alloc(n_pix) != cudaSuccess || h->out.alloc(n_pix) != cudaSuccess ||
       h->sens_point.alloc(n_pix) != cudaSuccess || h->sens_pixel.alloc(n_pix) != cudaSuccess ||
       h->counters.alloc(1) != cudaSuccess) {
@@ -629,7 +633,8 @@ int jpet_strip_destroy(jpet_strip_t* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   h->rho.release();
   h->out.release();
-  h->out64.release();
+  h->out_lo.release();
+  h->out_q.release();
   h->sens_point.release();
   h->sens_pixel.release();
   h->raw.release();
@@ -731,9 +736,13 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
   for (int it = 0; it < n; ++it) {
     JPET_CUDA(h, cudaMemsetAsync(h->out.p, 0, n_pix * sizeof(float), s), "clear image");
     JPET_CUDA(h, cudaMemsetAsync(h->counters.p, 0, sizeof(DevCounters), s), "clear counters");
-    const bool fixed = h->opts.precision != JPET_PRECISION_FP32;
-    if (fixed)
-      JPET_CUDA(h, cudaMemsetAsync(h->out64.p, 0, n_pix * sizeof(double), s), "clear image");
+    const bool aux_img = h->opts.precision != JPET_PRECISION_FP32;
+    const AuxImage aux{h->out_lo.p, h->out_q.p};
+    if (h->out_lo.p)
+      JPET_CUDA(h, cudaMemsetAsync(h->out_lo.p, 0, n_pix * sizeof(float), s), "clear image");
+    if (h->out_q.p)
+      JPET_CUDA(h, cudaMemsetAsync(h->out_q.p, 0, n_pix * sizeof(unsigned long long), s),
+                "clear image");
     if (h->use_fast) {
       const int prec = precision_code(h->opts.precision);
       const uint32_t seed = 0x9E3779B9u * static_cast<uint32_t>(h->iterations_done + 1);
@@ -746,14 +755,14 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
       } else if (h->opts.variant == JPET_VARIANT_WARP) {
         JPET_CUDA(h, launch_iterate_fast(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
                                          h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
-                                         h->rho.p, h->out.p, h->out64.p, h->counters.p, prec,
+                                         h->rho.p, h->out.p, aux, h->counters.p, prec,
                                          seed, s),
                   "iteration kernel launch");
       } else {
         JPET_CUDA(h, launch_iterate_rows(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
                                          h->sorted_geom.p, h->sorted_box.p, h->ev_pk.p,
                                          h->row_pk.p, h->row_pq.p, h->rho.p, h->out.p,
-                                         h->out64.p, h->counters.p, prec, seed, s),
+                                         aux, h->counters.p, prec, seed, s),
                   "iteration kernel launch");
       }
     } else {
@@ -765,8 +774,9 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
     JPET_CUDA(h, launch_iterate_global(h->g, h->opts.mode, h->n_oversize, h->over_geom.p,
                                        h->over_box.p, h->rho.p, sens, h->out.p, h->counters.p, s),
               "large-box kernel launch");
-    if (fixed)
-      JPET_CUDA(h, launch_combine_fixed(h->out64.p, h->out.p, h->out.p, n_pix, s),
+    if (aux_img)
+      JPET_CUDA(h, launch_combine_aux(precision_code(h->opts.precision), aux, h->out.p, h->out.p,
+                                      n_pix, s),
                 "combine kernel launch");
     std::swap(h->rho, h->out);
     ++h->iterations_done;

@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
     DevGeom g, FastConst fc, Tiling t, const Chunk* __restrict__ chunks,
     const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
     const uint16_t* __restrict__ rows, const float* __restrict__ rho, float* __restrict__ out,
-    double* __restrict__ out64, DevCounters* counters, uint32_t seed) {
+    AuxImage aux, DevCounters* counters, uint32_t seed) {
   extern __shared__ __align__(16) float smem[];
   const int pitch = fast_pitch(t);
   const int wfl = fast_window_floats(t);
@@ -351,11 +351,11 @@ __global__ void __launch_bounds__(256) iterate_fast_kernel(
       } else if (ACC == kAccCompensated) {
         const float v = w_out[r * pitch + col], cv = w_comp[r * pitch + col];
         if ((v != 0.0f || cv != 0.0f) && gy < g.n_y && gx < g.n_z)
-          atomicAdd(&out64[gy * g.n_z + gx], static_cast<double>(v) + static_cast<double>(cv));
+          flush_compensated(out, aux.lo, gy * g.n_z + gx, v, cv);
       } else {
         const uint32_t q = reinterpret_cast<const uint32_t*>(w_out)[r * pitch + col];
         if (q != 0u && gy < g.n_y && gx < g.n_z)
-          atomicAdd(&out64[gy * g.n_z + gx], static_cast<double>(q) * (1.0 / 4194304.0));
+          atomicAdd(&aux.q[gy * g.n_z + gx], static_cast<unsigned long long>(q));
       }
     }
   }
@@ -365,7 +365,7 @@ template <int RS, int SW, int ACC, bool DEN64>
 cudaError_t launch_fast_kernel(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                const short4* ev_box, const uint16_t* rows, const float* rho,
-                               float* out, double* out64, DevCounters* counters, uint32_t seed,
+                               float* out, AuxImage aux, DevCounters* counters, uint32_t seed,
                                cudaStream_t s) {
   const size_t smem =
       (ACC == kAccCompensated ? 3ull : 2ull) * fast_window_floats(t) * sizeof(float);
@@ -374,7 +374,7 @@ cudaError_t launch_fast_kernel(const DevGeom& g, const FastConst& fc, const Tili
                                          static_cast<int>(smem));
   if (err != cudaSuccess) return err;
   iterate_fast_kernel<RS, SW, ACC, DEN64><<<n_chunks, t.threads, smem, s>>>(
-      g, fc, t, chunks, ev_geom, ev_box, rows, rho, out, out64, counters, seed);
+      g, fc, t, chunks, ev_geom, ev_box, rows, rho, out, aux, counters, seed);
   return cudaGetLastError();
 }
 
@@ -382,31 +382,34 @@ template <int RS, int SW>
 cudaError_t launch_fast_shape(const DevGeom& g, const FastConst& fc, const Tiling& t,
                               const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                               const short4* ev_box, const uint16_t* rows, const float* rho,
-                              float* out, double* out64, DevCounters* counters, int precision,
+                              float* out, AuxImage aux, DevCounters* counters, int precision,
                               uint32_t seed, cudaStream_t s) {
   switch (precision) {
     case kPrecisionCompensated:
       return launch_fast_kernel<RS, SW, kAccCompensated, false>(
-          g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out, out64, counters, seed, s);
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out, aux, counters, seed, s);
     case kPrecisionCompensatedDen64:
       return launch_fast_kernel<RS, SW, kAccCompensated, true>(
-          g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out, out64, counters, seed, s);
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out, aux, counters, seed, s);
     case kPrecisionFixed:
       return launch_fast_kernel<RS, SW, kAccFixed, false>(g, fc, t, chunks, n_chunks, ev_geom,
-                                                          ev_box, rows, rho, out, out64, counters,
+                                                          ev_box, rows, rho, out, aux, counters,
                                                           seed, s);
     default:
       return launch_fast_kernel<RS, SW, kAccFloat, false>(g, fc, t, chunks, n_chunks, ev_geom,
-                                                          ev_box, rows, rho, out, out64, counters,
+                                                          ev_box, rows, rho, out, aux, counters,
                                                           seed, s);
   }
 }
 
-__global__ void combine_fixed_kernel(const double* __restrict__ out64,
-                                     const float* __restrict__ out_f, float* __restrict__ rho,
-                                     int64_t n) {
+__global__ void combine_aux_kernel(int fixed, AuxImage aux, const float* __restrict__ out,
+                                   float* __restrict__ rho, int64_t n) {
   int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n) rho[i] = static_cast<float>(out64[i] + static_cast<double>(out_f[i]));
+  if (i >= n) return;
+  if (fixed)  // one rounding from the exact integer sum, then an exact power-of-2 scale
+    rho[i] = __fadd_rn(__fmul_rn(__ull2float_rn(aux.q[i]), 1.0f / 4194304.0f), out[i]);
+  else
+    rho[i] = __fadd_rn(out[i], aux.lo[i]);
 }
 
 }  // namespace
@@ -499,27 +502,27 @@ cudaError_t launch_row_coefficients(const DevGeom& g, const FastConst& fc, const
 cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint16_t* rows, const float* rho,
-                                float* out, double* out64, DevCounters* counters, int precision,
+                                float* out, AuxImage aux, DevCounters* counters, int precision,
                                 uint32_t seed, cudaStream_t s) {
   if (n_chunks <= 0) return cudaSuccess;
   switch (t.fast_shape) {
     case kShapeS:
       return launch_fast_shape<4, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out,
-                                     out64, counters, precision, seed, s);
+                                     aux, counters, precision, seed, s);
     case kShapeM:
       return launch_fast_shape<8, 3>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho, out,
-                                     out64, counters, precision, seed, s);
+                                     aux, counters, precision, seed, s);
     default:
       return launch_fast_shape<12, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, rows, rho,
-                                      out, out64, counters, precision, seed, s);
+                                      out, aux, counters, precision, seed, s);
   }
 }
 
-cudaError_t launch_combine_fixed(const double* out64, const float* out_f, float* rho, int64_t n,
-                                 cudaStream_t s) {
+cudaError_t launch_combine_aux(int precision, AuxImage aux, const float* out, float* rho,
+                               int64_t n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  combine_fixed_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(out64, out_f, rho,
-                                                                             n);
+  combine_aux_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(
+      precision == kPrecisionFixed ? 1 : 0, aux, out, rho, n);
   return cudaGetLastError();
 }
 

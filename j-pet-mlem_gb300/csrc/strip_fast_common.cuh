@@ -53,15 +53,31 @@ struct FastLane {
 //              rounding error of every addition (Knuth's TwoSum) is added to a
 //              second, compensation window, so sum + compensation carries the
 //              tile total to second order (the compensated-summation idea of
-//              Kahan and Neumaier, made atomic); tiles go to an FP64 image.
+//              Kahan and Neumaier, made atomic); tiles go to an FP32 image and
+//              an FP32 compensation image (flush_compensated).
 //   kAccFixed: each contribution (a fraction of one event, in [0, 1]) rounded to
 //              22 fractional bits with an unbiased per-event dither and added
 //              with integer shared atomics; a window pixel of a chunk of <= 512
 //              events then stays below 2^31, and its sum is independent of the
-//              order of the additions (deterministic tiles).
+//              order of the additions; tiles go to a 64-bit integer image, so
+//              the whole image is deterministic.
 enum Acc : int { kAccFloat = 0, kAccCompensated = 1, kAccFixed = 2 };
 constexpr float kFixedScale = 4194304.0f;     // 2^22
 constexpr float kMagic = 12582912.0f;         // 1.5 * 2^23: float -> integer rounding
+
+// Tile flush of the compensated modes: the tile sum v goes into the FP32 image
+// with one float atomic; TwoSum of the value that atomic found and v recovers
+// the addition's exact rounding error (the atomic rounds to nearest), which
+// joins the tile's own compensation cv in the FP32 compensation image.
+__device__ __forceinline__ void flush_compensated(float* out, float* lo, int i, float v,
+                                                  float cv) {
+  const float old = atomicAdd(out + i, v);
+  const float sum = __fadd_rn(old, v);
+  const float bp = __fsub_rn(sum, old);
+  const float err = __fadd_rn(__fsub_rn(old, __fsub_rn(sum, bp)), __fsub_rn(v, bp));
+  const float c = __fadd_rn(err, cv);
+  if (c != 0.0f) atomicAdd(lo + i, c);
+}
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
   // integer finaliser of MurmurHash3 (public domain, Austin Appleby)

@@ -116,9 +116,18 @@ cudaError_t launch_fill(float* p, float v, int64_t n, cudaStream_t s);
 cudaError_t launch_row_tables(const DevGeom& g, const Tiling& t, int32_t n_events,
                               const float4* ev_geom, const short4* ev_box, uint16_t* rows,
                               unsigned long long* kernel_calls, cudaStream_t s);
+// Second image of the compensated and fixed-point modes: the FP32 compensation
+// image (the exact rounding errors of the main image's additions, summed) or
+// the 64-bit fixed-point image (units of 2^-22 of an event; integer sums are
+// exact and independent of their order).
+struct AuxImage {
+  float* lo;
+  unsigned long long* q;
+};
 // Accumulation of the fast kernel: float shared atomics; compensated tile sums
-// flushed into an FP64 image (optionally with FP64 denominators); or
-// deterministic fixed-point tile sums flushed into an FP64 image.
+// flushed into an FP32 image and its FP32 compensation image (optionally with
+// FP64 denominators); or fixed-point tile sums flushed into a 64-bit integer
+// image (deterministic).
 enum FastPrecision : int32_t {
   kPrecisionFloat = 0,
   kPrecisionCompensated = 1,
@@ -144,7 +153,7 @@ cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Til
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint32_t* ev_pk,
                                 const uint32_t* rows, const float2* pq, const float* rho,
-                                float* out, double* out64, DevCounters* counters,
+                                float* out, AuxImage aux, DevCounters* counters,
                                 int precision, uint32_t seed, cudaStream_t s);
 // Set-up order of the events (strip_sort.cu): radix sort by tile, box corner
 // and tan, then a gather into the tile-sorted and oversize arrays.
@@ -173,7 +182,7 @@ cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Ti
 cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint16_t* rows, const float* rho,
-                                float* out, double* out64, DevCounters* counters, int precision,
+                                float* out, AuxImage aux, DevCounters* counters, int precision,
                                 uint32_t seed, cudaStream_t s);
 // Constants of the likelihood adjoint at the kernel sigmas (strip_adjoint.cu).
 struct NllConst {
@@ -191,9 +200,11 @@ cudaError_t launch_nll_grad(const DevGeom& g, const NllConst& k, const Tiling& t
 // acc[0] += sum s rho; grad += s (grad may be null)
 cudaError_t launch_nll_finish(const float* sens, const float* rho, float* grad, double* acc,
                               int64_t n, cudaStream_t s);
-// rho = float(out64 + out_f)
-cudaError_t launch_combine_fixed(const double* out64, const float* out_f, float* rho, int64_t n,
-                                 cudaStream_t s);
+// The image of an iteration in the compensated and fixed-point modes:
+// rho = out + aux.lo (compensated) or rho = float(aux.q 2^-22) + out (fixed;
+// out holds the contributions of events taken by the reference-order paths).
+cudaError_t launch_combine_aux(int precision, AuxImage aux, const float* out, float* rho,
+                               int64_t n, cudaStream_t s);
 cudaError_t launch_iterate(const DevGeom& g, const Tiling& t, int32_t semantics,
                            const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                            const short4* ev_box, const float* rho, const float* sens,

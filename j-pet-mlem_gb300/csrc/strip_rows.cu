@@ -65,7 +65,7 @@ __device__ __forceinline__ void rows_chunk(
     const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
     const uint32_t* __restrict__ ev_pk, const uint32_t* __restrict__ rows,
     const float2* __restrict__ row_pq, const float* __restrict__ rho, float* __restrict__ out,
-    double* __restrict__ out64, DevCounters* counters, uint32_t seed) {
+    AuxImage aux, DevCounters* counters, uint32_t seed) {
   constexpr int kRowsPerWarp = 32 / G;       // rows of one warp step
   constexpr int kPass = NW * kRowsPerWarp;   // event rows covered by one step of all warps
   constexpr int kSweep = 2 * G;              // columns per sweep
@@ -345,11 +345,11 @@ __device__ __forceinline__ void rows_chunk(
       } else if (ACC == kAccCompensated) {
         const float v = w_out[r * pitch + col], cv = w_comp[r * pitch + col];
         if ((v != 0.0f || cv != 0.0f) && gy < g.n_y && gx < g.n_z)
-          atomicAdd(&out64[gy * g.n_z + gx], static_cast<double>(v) + static_cast<double>(cv));
+          flush_compensated(out, aux.lo, gy * g.n_z + gx, v, cv);
       } else {
         const uint32_t q = reinterpret_cast<const uint32_t*>(w_out)[r * pitch + col];
         if (q != 0u && gy < g.n_y && gx < g.n_z)
-          atomicAdd(&out64[gy * g.n_z + gx], static_cast<double>(q) * (1.0 / 4194304.0));
+          atomicAdd(&aux.q[gy * g.n_z + gx], static_cast<unsigned long long>(q));
       }
     }
   }
@@ -361,9 +361,9 @@ __global__ void __launch_bounds__(NW * 32, (NW == 8 ? 2 : 4)) iterate_rows_kerne
     const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
     const uint32_t* __restrict__ ev_pk, const uint32_t* __restrict__ rows,
     const float2* __restrict__ row_pq, const float* __restrict__ rho, float* __restrict__ out,
-    double* __restrict__ out64, DevCounters* counters, uint32_t seed) {
+    AuxImage aux, DevCounters* counters, uint32_t seed) {
   rows_chunk<NW, G, RS, SW, E, ACC, DEN64>(g, fc, t, chunks[blockIdx.x], ev_geom, ev_box, ev_pk,
-                                           rows, row_pq, rho, out, out64, counters, seed);
+                                           rows, row_pq, rho, out, aux, counters, seed);
 }
 
 // Shapes name the rows an event may span (kPass * RS): the warps per CTA set
@@ -374,7 +374,7 @@ cudaError_t launch_rows_kernel(const DevGeom& g, const FastConst& fc, const Tili
                                int32_t n_chunks, const float4* ev_geom, const short4* ev_box,
                                const uint32_t* ev_pk, const uint32_t* rows, const float2* pq,
                                const float* rho,
-                               float* out, double* out64, DevCounters* counters, uint32_t seed,
+                               float* out, AuxImage aux, DevCounters* counters, uint32_t seed,
                                cudaStream_t s, int op) {
   constexpr int kPass = NW * (32 / G);
   constexpr int RS = (ROWS + kPass - 1) / kPass;
@@ -386,7 +386,7 @@ cudaError_t launch_rows_kernel(const DevGeom& g, const FastConst& fc, const Tili
     return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 static_cast<int>(smem));
   k<<<n_chunks, NW * 32, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out,
-                                    out64, counters, seed);
+                                    aux, counters, seed);
   return cudaGetLastError();
 }
 
@@ -395,24 +395,24 @@ cudaError_t launch_rows_prec(const DevGeom& g, const FastConst& fc, const Tiling
                              const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                              const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
                               const float2* pq,
-                             const float* rho, float* out, double* out64, DevCounters* counters,
+                             const float* rho, float* out, AuxImage aux, DevCounters* counters,
                              int precision, uint32_t seed, cudaStream_t s, int op) {
   switch (precision) {
     case kPrecisionCompensated:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccCompensated, false>(
-          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, aux, counters, seed,
           s, op);
     case kPrecisionCompensatedDen64:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccCompensated, true>(
-          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, aux, counters, seed,
           s, op);
     case kPrecisionFixed:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccFixed, false>(
-          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, aux, counters, seed,
           s, op);
     default:
       return launch_rows_kernel<NW, G, ROWS, SW, kAccFloat, false>(
-          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, out64, counters, seed,
+          g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out, aux, counters, seed,
           s, op);
   }
 }
@@ -424,13 +424,13 @@ cudaError_t launch_rows_shape(const DevGeom& g, const FastConst& fc, const Tilin
                               const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                               const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
                               const float2* pq,
-                              const float* rho, float* out, double* out64, DevCounters* counters,
+                              const float* rho, float* out, AuxImage aux, DevCounters* counters,
                               int precision, uint32_t seed, cudaStream_t s, int op) {
   if (t.threads == 256)
     return launch_rows_prec<8, G, ROWS, SW>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq,
-                                            rho, out, out64, counters, precision, seed, s, op);
+                                            rho, out, aux, counters, precision, seed, s, op);
   return launch_rows_prec<4, G, ROWS, SW>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq,
-                                          rho, out, out64, counters, precision, seed, s, op);
+                                          rho, out, aux, counters, precision, seed, s, op);
 }
 
 // ---- batched reconstructions ------------------------------------------------------
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(NW * 32, (NW == 8 ? 2 : 4))
     const BatchInstance& in = insts[w.inst];
     rows_chunk<NW, G, RS, SW, E, kAccFloat, false>(
         in.g, in.fc, in.t, in.chunks[w.index], in.ev_geom, in.ev_box, in.ev_pk, in.rows, in.pq,
-        in.img[parity], in.img[parity ^ 1], nullptr, in.counters, 0u);
+        in.img[parity], in.img[parity ^ 1], AuxImage{}, in.counters, 0u);
     __syncthreads();
   }
 }
@@ -563,7 +563,7 @@ static cudaError_t rows_dispatch(const DevGeom& g, const FastConst& fc, const Ti
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
                               const float2* pq,
-                                const float* rho, float* out, double* out64,
+                                const float* rho, float* out, AuxImage aux,
                                 DevCounters* counters, int precision, uint32_t seed,
                                 cudaStream_t s, int op) {
   if (op != 0 && n_chunks <= 0) return cudaSuccess;
@@ -571,41 +571,41 @@ static cudaError_t rows_dispatch(const DevGeom& g, const FastConst& fc, const Ti
   switch (t.rows_shape) {
     case kRowsShape8x1x1:
       return launch_rows_shape<8, 32, 1>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s, op);
+                                         out, aux, counters, precision, seed, s, op);
     case kRowsShape8x1x2:
       return launch_rows_shape<8, 32, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s, op);
+                                         out, aux, counters, precision, seed, s, op);
     case kRowsShape4x1x2:
       return launch_rows_shape<4, 64, 2>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s, op);
+                                         out, aux, counters, precision, seed, s, op);
     case kRowsShape4x1x3:
       return launch_rows_shape<4, 64, 3>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s, op);
+                                         out, aux, counters, precision, seed, s, op);
     case kRowsShape4x1x4:
       return launch_rows_shape<4, 64, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s, op);
+                                         out, aux, counters, precision, seed, s, op);
     case kRowsShape2x1x6:
       return launch_rows_shape<2, 64, 6>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                         out, out64, counters, precision, seed, s, op);
+                                         out, aux, counters, precision, seed, s, op);
     default:
       return launch_rows_shape<4, 128, 4>(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho,
-                                          out, out64, counters, precision, seed, s, op);
+                                          out, aux, counters, precision, seed, s, op);
   }
 }
 
 cudaError_t launch_iterate_rows(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint32_t* ev_pk, const uint32_t* rows,
-                                const float2* pq, const float* rho, float* out, double* out64,
+                                const float2* pq, const float* rho, float* out, AuxImage aux,
                                 DevCounters* counters, int precision, uint32_t seed,
                                 cudaStream_t s) {
   return rows_dispatch(g, fc, t, chunks, n_chunks, ev_geom, ev_box, ev_pk, rows, pq, rho, out,
-                       out64, counters, precision, seed, s, 1);
+                       aux, counters, precision, seed, s, 1);
 }
 
 cudaError_t rows_prepare_kernel(const Tiling& t, int precision) {
   return rows_dispatch(DevGeom{}, FastConst{}, t, nullptr, 0, nullptr, nullptr, nullptr, nullptr,
-                       nullptr, nullptr, nullptr, nullptr, nullptr, precision, 0u, nullptr, 0);
+                       nullptr, nullptr, nullptr, AuxImage{}, nullptr, precision, 0u, nullptr, 0);
 }
 
 size_t rows_smem_bytes(const Tiling& t, int threads, int rows_shape) {

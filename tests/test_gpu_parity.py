@@ -434,3 +434,19 @@ def test_fine_pixels_with_boxes_beyond_every_shape(variant):
     assert cnt["n_contributing"] == st["n_contributing"]
     if variant != capi.VARIANT_EXACT:
         assert cnt["n_oversize"] + cnt["n_exact_path"] > 0, cnt
+
+
+def test_fixed_point_mode_is_deterministic(golden):
+    """Fixed-point tiles summed into the 64-bit integer image: two runs give the
+    same image bit for bit (integer sums do not depend on their order)."""
+    manifest, load = golden
+    cg, _ = _geoms(manifest["c1"])
+    ev = load("c1_events.npy")
+    imgs = []
+    for _ in range(2):
+        with capi.StripReconstruction(cg, precision=capi.PRECISION_FIXED) as rec:
+            rec.set_events(ev)
+            rec.iterate(3)
+            assert rec.counters()["n_exact_path"] == 0 and rec.counters()["n_oversize"] == 0
+            imgs.append(rec.rho.copy())
+    assert np.array_equal(imgs[0], imgs[1])
