@@ -14,6 +14,8 @@
 #               restatement reproduces bit for bit.
 #   ref_phantom the reference `2d_strip_phantom` event generator (same recipe).
 #   ref_fp64    ref_fp64_harness.cpp: the reference Reconstruction template at double.
+#   ref_analytic ref_analytic_harness.cpp: the reference AnalyticKernel and
+#               Scanner::pixel_sensitivity at float and double (no FP contraction).
 #   ref_convert the reference `3d_tool_convert` (src/3d/tool/convert_cmd.cpp with the
 #               barrel and hybrid option files); MAX_DETECTORS=400 as the reference's
 #               CMakeLists.txt:19 sets it.
@@ -61,6 +63,8 @@ $CXX $COMMON -o "$OUT/ref_phantom" \
   "$REF/src/2d/strip/phantom_cmd.cpp" "$REF/src/2d/strip/options.cpp" \
   $HELPERS -ldl &
 $CXX $COMMON -ffp-contract=off -o "$OUT/ref_fp64" "$HERE/ref_fp64_harness.cpp" &
+$CXX $COMMON -ffp-contract=off -o "$OUT/ref_analytic" "$HERE/ref_analytic_harness.cpp" &
+$CXX $COMMON -ffp-contract=off -o "$OUT/ref_analytic" "$HERE/ref_analytic_harness.cpp" &
 $CXX $COMMON -DMAX_DETECTORS=400 -o "$OUT/ref_convert" \
   "$REF/src/3d/tool/convert_cmd.cpp" "$REF/src/3d/tool/options.cpp" \
   "$REF/src/2d/barrel/options.cpp" "$REF/src/3d/hybrid/options.cpp" $HELPERS -ldl &
