@@ -69,6 +69,11 @@ def parse():
                    help="events of the prefix iterated against the reference float path")
     p.add_argument("--accuracy-report", action="store_true",
                    help="every iteration of the full workload against the FP64 GPU iteration")
+    p.add_argument("--calibration-report", action="store_true",
+                   help="blind width recalibration on the differentiable configuration")
+    p.add_argument("--adjoint-report", action="store_true",
+                   help="the adjoint entry alone (loss + gradient timing, no calibration)")
+    p.add_argument("--adjoint-events", type=int, default=5_000_000)
     p.add_argument("--precision-report", action="store_true",
                    help="print the precision-stress comparison instead of the headline line")
     p.add_argument("--variant", type=int, default=0,
@@ -355,7 +360,7 @@ def gb300_arm(args, wl, world, rank, local):
     adjoint = None
     if not args.no_adjoint:
         try:
-            adjoint = adjoint_summary(local)
+            adjoint = adjoint_summary(local, ex2_peak=(peaks or {}).get("ex2_per_s"))
         except Exception as exc:  # reported, the headline line still prints
             adjoint = {"error": f"{type(exc).__name__}: {exc}"}
     hbm, hbm_kind = hbm_peak()
@@ -609,6 +614,32 @@ def accuracy_full_report(args, wl, local):
 
 
 
+def calibration_report(local):
+    """bench.py --calibration-report: the differentiable configuration as stated
+    (500 x 450 at 2 mm, 5e6 events of the seeded 10-ellipse phantom simulated
+    with sigma (10, 42)), widths fitted blind -- MLEM image at the current
+    widths from half the events, widths fitted to the other half -- from the
+    mis-specified (14, 55) and, as a control, from the true (10, 42).  Prints
+    the trajectories; with the activity image unknown the widths are not
+    identifiable (a blurred image under narrower widths predicts the same
+    events), which these runs measure."""
+    from jpet_strip import capi, phantom
+    from jpet_strip.autograd import recalibrate_sigma
+
+    ev = capi.generate(phantom.random_ellipse_phantom(seed=3), 5_000_000, 450.0, 1000.0,
+                       10.0, 42.0, seed=3, device=local)
+    out = {"config": {"grid": "500x450", "pixel_mm": 2.0, "events": len(ev),
+                      "true_sigma": [10.0, 42.0], "phantom": "random10, seed 3"}}
+    for label, start in (("from_14_55", (14.0, 55.0)), ("from_true_10_42", (10.0, 42.0))):
+        geom = capi.Geometry(450.0, 1000.0, 450, 500, 2.0, *start)
+        t0 = time.perf_counter()
+        sigma, hist = recalibrate_sigma(geom, ev, start, outer=12, device=local)
+        out[label] = {"start": list(start), "final": [float(sigma[0]), float(sigma[1])],
+                      "seconds": time.perf_counter() - t0,
+                      "trajectory": [h["sigma"] for h in hist]}
+    print(json.dumps(out), flush=True)
+
+
 def profile_traffic(n_events, key="dram_bytes_per_launch", variant=0):
     """DRAM bytes (or warp instructions, key "warp_instructions_per_launch") per
     iteration-kernel launch from the committed ncu capture of the kernel the
@@ -720,7 +751,7 @@ def batch_summary(local, iterations=10, k=64):
     return out
 
 
-def adjoint_summary(local, n_events=5_000_000):
+def adjoint_summary(local, n_events=5_000_000, ex2_peak=None, calibrate=True):
     """Differentiable form: 5e6 events of a centred point source simulated with
     sigma (10, 42) on the 2 mm grid.  Times one loss + gradient evaluation
     (dL/drho image and dL/dsigma) at the mis-specified widths (14, 55), then
@@ -740,6 +771,8 @@ def adjoint_summary(local, n_events=5_000_000):
     grad = torch.empty_like(rho)
     with capi.StripReconstruction(geom, device=local) as rec:
         rec.set_events(ev)
+        rec.iterate(1)  # counts the kernel evaluations of the supports at (14, 55)
+        evals = rec.counters()["n_kernel_calls"]
         rec.nll_grad(14.0, 55.0, rho.data_ptr(), None, grad.data_ptr())  # warm-up
         torch.cuda.synchronize()
         reps = 5
@@ -747,15 +780,25 @@ def adjoint_summary(local, n_events=5_000_000):
         for _ in range(reps):
             loss, gs, skipped = rec.nll_grad(14.0, 55.0, rho.data_ptr(), None, grad.data_ptr())
         dt = (time.perf_counter() - t0) / reps
-    t0 = time.perf_counter()
-    sigma, hist = calibrate_sigma(geom, ev, img, (14.0, 55.0), device=local)
-    cal_s = time.perf_counter() - t0
-    return {"events": n_events, "grid": "500x450", "pixel_mm": 2.0,
-            "true_sigma": [10.0, 42.0], "start_sigma": [14.0, 55.0],
-            "loss_and_gradient_ms": 1e3 * dt, "events_per_s": n_events / dt,
-            "recovered_sigma": [float(sigma[0]), float(sigma[1])],
-            "calibration_steps": len(hist), "calibration_seconds": cal_s,
-            "within_0p5_mm": bool(abs(sigma[0] - 10.0) < 0.5 and abs(sigma[1] - 42.0) < 0.5)}
+    out = {"events": n_events, "grid": "500x450", "pixel_mm": 2.0,
+           "true_sigma": [10.0, 42.0], "start_sigma": [14.0, 55.0],
+           "loss_and_gradient_ms": 1e3 * dt, "events_per_s": n_events / dt,
+           "kernel_evaluations": int(evals), "evals_per_s": evals / dt}
+    if ex2_peak:
+        # each evaluation needs one exp of K and its sigma derivatives
+        out["roofline"] = {"bound": "sfu", "achieved": evals / dt / 1e9, "peak": ex2_peak / 1e9,
+                           "unit": "Gex2/s", "frac": evals / dt / ex2_peak,
+                           "note": "FP64 row terms and sigma derivatives per evaluation; the "
+                                   "kernel is bound by FP64 and FP32 issue, not the SFU"}
+    if calibrate:
+        t0 = time.perf_counter()
+        sigma, hist = calibrate_sigma(geom, ev, img, (14.0, 55.0), device=local)
+        cal_s = time.perf_counter() - t0
+        out.update({"recovered_sigma": [float(sigma[0]), float(sigma[1])],
+                    "calibration_steps": len(hist), "calibration_seconds": cal_s,
+                    "within_0p5_mm": bool(abs(sigma[0] - 10.0) < 0.5 and
+                                          abs(sigma[1] - 42.0) < 0.5)})
+    return out
 
 
 def precision_report(args, local):
@@ -847,6 +890,11 @@ def main():
         precision_report(args, local)
     elif args.accuracy_report:
         accuracy_full_report(args, wl, local)
+    elif args.calibration_report:
+        calibration_report(local)
+    elif args.adjoint_report:
+        print(json.dumps({"adjoint": adjoint_summary(local, args.adjoint_events,
+                                                     calibrate=False)}), flush=True)
     else:
         gb300_arm(args, wl, world, rank, local)
 

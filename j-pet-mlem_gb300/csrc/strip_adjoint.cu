@@ -26,7 +26,9 @@
 // One warp per event; each row's exact in-ellipse interval is found with the
 // same search as the MLEM row tables (row_interval), so the support is exactly
 // the reference's.  The rows' constants are set up 32 at a time, one row per
-// lane, and broadcast to the warp for the row's pixels.  For the events of the tiled chunks the rho window and a
+// lane, and broadcast to the warp for the row's pixels; the constants of the
+// first 128 rows are kept in registers for the second (gradient) pass.  For the
+// events of the tiled chunks the rho window and a
 // gradient window live in shared memory (as in the MLEM kernel); events whose
 // box exceeds the windows use the global image.  Per-event log-likelihood and
 // sigma-derivative terms are reduced in FP64 per CTA.
@@ -73,6 +75,63 @@ __device__ __forceinline__ void nll_event(const DevGeom& g, const NllConst& k, f
   const double kdl_sec2 = k.kdl_d * sec2;
   const int nrows = box.w - box.y;
   float den = 0.0f, dz = 0.0f, ddl = 0.0f, inv = 0.0f;
+  // lane l sets up row rb + l: exact interval and FP64 row term
+  struct RowConst {
+    int first, w;
+    float arg, cz, cdl, u;
+  };
+  auto setup = [&](int rb) {
+    RowConst c{0, 0, 0.0f, 0.0f, 0.0f, 0.0f};
+    const int ri = rb + lane;
+    if (ri < nrows) {
+      const int iy = box.y + ri;
+      c.w = row_interval(g, A, B, C, z, y, tn, sec, box.x, box.z, iy, c.first);
+      const float py = g.tl_y_half_h - static_cast<float>(iy) * g.pixel_height;
+      const float dy = py - y;
+      const float pa = pa_c * (py * py + g.radius * g.radius), qa = qa_c * py * py;
+      const float ama = pa * k.ipz + qa * k.ipd;
+      const double dyd = dy;
+      c.arg = static_cast<float>(-0.5 * kNllLog2e * log1p(qq * dyd * (static_cast<double>(py) + y)) +
+                                 kdl_sec2 * dyd * dyd);
+      c.cz = k.inv_ipz - 0.5f * pa / ama;
+      c.cdl = k.half_inv_ipd - 0.5f * qa / ama - 2.0f * sec2 * dy * dy;
+      c.u = g.tl_z_half_w - z - dy * tn;
+    }
+    return c;
+  };
+  // the warp sweeps the group's rows one by one with the constants broadcast
+  // from their lanes: forward sums (pass 0) or gradient contributions (pass 1)
+  auto sweep = [&](int pass, int rb, const RowConst& c) {
+    const int n_group = min(32, nrows - rb);
+    for (int r = 0; r < n_group; ++r) {
+      const int wr = __shfl_sync(kFull, c.w, r);
+      if (wr == 0) continue;
+      const int fr = __shfl_sync(kFull, c.first, r);
+      const float ra = __shfl_sync(kFull, c.arg, r);
+      const float czr = __shfl_sync(kFull, c.cz, r);
+      const float cdr = __shfl_sync(kFull, c.cdl, r);
+      const float ur = __shfl_sync(kFull, c.u, r);
+      const int iy = box.y + rb + r;
+      for (int j = lane; j < wr; j += 32) {
+        const int col = fr + j;
+        const float u = fmaf(static_cast<float>(col), g.pixel_width, ur);
+        const float kv = exp2f(fmaf(k.kz * u, u, fmaf(k.kz_lo * u, u, ra)));
+        const int wi = wv.index(iy, col);
+        if (pass == 0) {
+          const float kr = kv * wv.rho[wi];
+          den += kr;
+          dz += kr * (czr - u * u);
+          ddl += kr * cdr;
+        } else {
+          atomicAdd(&wv.grad[wi], -kv * inv);
+        }
+      }
+    }
+  };
+  // the constants of up to kCachedGroups x 32 rows stay in registers between
+  // the two passes; taller boxes set their rows up again in the second pass
+  constexpr int kCachedGroups = 4;
+  RowConst cache[kCachedGroups];
   for (int pass = 0; pass < 2; ++pass) {
     if (pass == 1) {
       dz *= k.dipz_dsz;
@@ -96,52 +155,17 @@ __device__ __forceinline__ void nll_event(const DevGeom& g, const NllConst& k, f
       }
       inv = static_cast<float>(1.0 / dd);
     }
-    // rows in groups of 32: lane l sets up row rb + l (exact interval, FP64 row
-    // term), then the warp sweeps the group's rows one by one with the
-    // constants broadcast from their lanes
+#pragma unroll 1
     for (int rb = 0; rb < nrows; rb += 32) {
-      const int ri = rb + lane;
-      int first = 0, w = 0;
-      float row_arg = 0.0f, cz = 0.0f, cdl = 0.0f, u_row = 0.0f;
-      if (ri < nrows) {
-        const int iy = box.y + ri;
-        w = row_interval(g, A, B, C, z, y, tn, sec, box.x, box.z, iy, first);
-        const float py = g.tl_y_half_h - static_cast<float>(iy) * g.pixel_height;
-        const float dy = py - y;
-        const float pa = pa_c * (py * py + g.radius * g.radius), qa = qa_c * py * py;
-        const float ama = pa * k.ipz + qa * k.ipd;
-        const double dyd = dy;
-        row_arg = static_cast<float>(-0.5 * kNllLog2e * log1p(qq * dyd * (static_cast<double>(py) + y)) +
-                                     kdl_sec2 * dyd * dyd);
-        cz = k.inv_ipz - 0.5f * pa / ama;
-        cdl = k.half_inv_ipd - 0.5f * qa / ama - 2.0f * sec2 * dy * dy;
-        u_row = g.tl_z_half_w - z - dy * tn;
+      const int gi = rb >> 5;
+      RowConst c;
+      if (gi >= kCachedGroups || pass == 0) {
+        c = setup(rb);
+        if (gi < kCachedGroups) cache[gi] = c;
+      } else {
+        c = cache[gi];
       }
-      const int n_group = min(32, nrows - rb);
-      for (int r = 0; r < n_group; ++r) {
-        const int wr = __shfl_sync(kFull, w, r);
-        if (wr == 0) continue;
-        const int fr = __shfl_sync(kFull, first, r);
-        const float ra = __shfl_sync(kFull, row_arg, r);
-        const float czr = __shfl_sync(kFull, cz, r);
-        const float cdr = __shfl_sync(kFull, cdl, r);
-        const float ur = __shfl_sync(kFull, u_row, r);
-        const int iy = box.y + rb + r;
-        for (int j = lane; j < wr; j += 32) {
-          const int col = fr + j;
-          const float u = fmaf(static_cast<float>(col), g.pixel_width, ur);
-          const float kv = exp2f(fmaf(k.kz * u, u, fmaf(k.kz_lo * u, u, ra)));
-          const int wi = wv.index(iy, col);
-          if (pass == 0) {
-            const float kr = kv * wv.rho[wi];
-            den += kr;
-            dz += kr * (czr - u * u);
-            ddl += kr * cdr;
-          } else {
-            atomicAdd(&wv.grad[wi], -kv * inv);
-          }
-        }
-      }
+      sweep(pass, rb, c);
     }
   }
 }
