@@ -16,6 +16,8 @@
 #   ref_fp64    ref_fp64_harness.cpp: the reference Reconstruction template at double.
 #   ref_analytic ref_analytic_harness.cpp: the reference AnalyticKernel and
 #               Scanner::pixel_sensitivity at float and double (no FP contraction).
+#   ref_hybrid  ref_hybrid_harness.cpp: the reference 3D hybrid Reconstruction
+#               (src/3d/hybrid/reconstruction.h) on one thread, no FP contraction.
 #   ref_convert the reference `3d_tool_convert` (src/3d/tool/convert_cmd.cpp with the
 #               barrel and hybrid option files); MAX_DETECTORS=400 as the reference's
 #               CMakeLists.txt:19 sets it.
@@ -50,6 +52,9 @@ COMMON="-std=c++11 -O3 $ARCHFLAG -fopenmp -include cstdint -w \
   -I$REF/src -I$REF/lib/cmdline -I$REF/lib/json \
   -DUSE_FAST_TEXT_PARSER=1 -DUSE_SENSITIVITY=1 -DUSE_KERNEL=1 \
   -DUSE_STATISTICS=0 -DWARP_SIZE=32"
+# the hybrid harness runs its event loop on one thread: no OpenMP
+SERIAL="-std=c++11 -O3 $ARCHFLAG -include cstdint -w -I$REF/src -I$REF/lib/cmdline \
+  -I$REF/lib/json -DUSE_FAST_TEXT_PARSER=1 -DMAX_DETECTORS=400 -DWARP_SIZE=32"
 HELPERS="$REF/src/common/options.cpp $REF/src/util/cmdline_hooks.cpp \
   $REF/src/util/backtrace.cpp $REF/src/util/string.cpp $HERE/ref_png_stub.cpp"
 
@@ -64,7 +69,7 @@ $CXX $COMMON -o "$OUT/ref_phantom" \
   $HELPERS -ldl &
 $CXX $COMMON -ffp-contract=off -o "$OUT/ref_fp64" "$HERE/ref_fp64_harness.cpp" &
 $CXX $COMMON -ffp-contract=off -o "$OUT/ref_analytic" "$HERE/ref_analytic_harness.cpp" &
-$CXX $COMMON -ffp-contract=off -o "$OUT/ref_analytic" "$HERE/ref_analytic_harness.cpp" &
+$CXX $SERIAL -ffp-contract=off -o "$OUT/ref_hybrid" "$HERE/ref_hybrid_harness.cpp" &
 $CXX $COMMON -DMAX_DETECTORS=400 -o "$OUT/ref_convert" \
   "$REF/src/3d/tool/convert_cmd.cpp" "$REF/src/3d/tool/options.cpp" \
   "$REF/src/2d/barrel/options.cpp" "$REF/src/3d/hybrid/options.cpp" $HELPERS -ldl &

@@ -242,3 +242,111 @@ def ref_binary(name: str) -> str | None:
     """Path of a reference tool built by build_ref.sh, if present on this host."""
     p = os.path.join(REF_DIR, name)
     return p if os.path.exists(p) and os.access(p, os.X_OK) else None
+
+
+# ---- 3D hybrid reconstruction (src/3d/hybrid/reconstruction.h) -----------------
+
+class OrcHybrid(C.Structure):
+    _fields_ = [
+        ("n_detectors", C.c_int32),
+        ("n_pixel_infos", C.c_int64),
+        ("segments", C.c_void_p),
+        ("lor_widths", C.c_void_p),
+        ("pixels", C.c_void_p),
+        ("positions", C.c_void_p),
+        ("info_begin", C.c_void_p),
+        ("info_end", C.c_void_p),
+        ("n_columns", C.c_int32),
+        ("n_rows", C.c_int32),
+        ("n_planes", C.c_int32),
+        ("pixel_size", C.c_float),
+        ("lower_left_x", C.c_float),
+        ("lower_left_y", C.c_float),
+        ("z_left", C.c_float),
+        ("sigma_z", C.c_float),
+        ("sigma_dl", C.c_float),
+        ("length", C.c_float),
+    ]
+
+
+def _hyb_lib():
+    L = lib()
+    if not hasattr(L, "_hyb_ready"):
+        hp = C.POINTER(OrcHybrid)
+        vp = C.c_void_p
+        L.orc_hybrid_calculate_weight.argtypes = [hp, vp]
+        L.orc_hybrid_calculate_sensitivity.argtypes = [hp, vp, vp]
+        L.orc_hybrid_normalize.argtypes = [hp, vp, vp]
+        L.orc_hybrid_translate_all.argtypes = [hp, vp, C.c_int64, vp, vp]
+        L.orc_hybrid_translate_all.restype = C.c_int64
+        L.orc_hybrid_mlem.argtypes = [hp, vp, vp, vp, C.c_int64, vp, C.c_int, C.c_int, vp]
+        L.orc_hybrid_mlem.restype = C.c_int
+        L._hyb_ready = True
+    return L
+
+
+def _ptr(a) -> int:
+    return a.ctypes.data if a.size else 0
+
+
+def hybrid_struct(g) -> tuple[OrcHybrid, list]:
+    """orc_hybrid view of a HybridGeometry (arrays kept alive by the returned list)."""
+    keep = [np.ascontiguousarray(a) for a in (g.segments, g.widths, g.pixels, g.positions,
+                                               g.info_begin, g.info_end)]
+    s = OrcHybrid(g.n_detectors, g.n_pixel_infos, *[_ptr(a) for a in keep], g.n_columns,
+                  g.n_rows, g.n_planes, g.pixel_size, g.lower_left_x, g.lower_left_y, g.z_left,
+                  g.sigma_z, g.sigma_dl, g.length)
+    return s, keep
+
+
+def hybrid_setup(g, weights_given: bool = False, sens_to_one: bool = False):
+    """calculate_weight (unless given), calculate_sensitivity or ones, and
+    normalize_geometry_weights: (normalized weights, raw 2D sensitivity)."""
+    L = _hyb_lib()
+    s, keep = hybrid_struct(g)
+    w = np.array(g.weights, np.float32, copy=True)
+    if not weights_given:
+        L.orc_hybrid_calculate_weight(C.byref(s), _ptr(w))
+    sens = np.ones(g.n_columns * g.n_rows, np.float32)
+    if not sens_to_one:
+        L.orc_hybrid_calculate_sensitivity(C.byref(s), _ptr(w), _ptr(sens))
+    L.orc_hybrid_normalize(C.byref(s), _ptr(w), _ptr(sens))
+    return w, sens
+
+
+def hybrid_translate(g, weights, responses):
+    """Frame events of the kept responses (translate_to_frame + bounding-box filter)."""
+    L = _hyb_lib()
+    s, keep = hybrid_struct(g)
+    r = np.ascontiguousarray(responses)
+    out = np.zeros(r.shape[0], dtype=_frame_dtype())
+    w = np.ascontiguousarray(weights, np.float32)
+    n = L.orc_hybrid_translate_all(C.byref(s), _ptr(r), r.shape[0], _ptr(w), _ptr(out))
+    return out[:n].copy()
+
+
+def _frame_dtype():
+    return np.dtype({
+        "names": ["first", "second", "up", "right", "tan", "sec", "info_begin", "info_end",
+                  "plane_begin", "plane_end"],
+        "formats": ["<i2", "<i2", "<f4", "<f4", "<f4", "<f4", "<u8", "<u8", "<i2", "<i2"],
+        "offsets": [0, 2, 4, 8, 12, 16, 24, 32, 40, 42],
+        "itemsize": 48})
+
+
+def hybrid_mlem(g, weights, sens, events, n_iterations: int, rho=None, threads: int = 1):
+    """n_iterations of Reconstruction::operator(); returns (rho float32[n_voxels],
+    counters int64[4]: used_events, used_pixels, used_voxels, positive denominators)."""
+    L = _hyb_lib()
+    s, keep = hybrid_struct(g)
+    rho = (np.ones(g.n_voxels, np.float32) if rho is None
+           else np.array(rho, np.float32, copy=True).reshape(-1))
+    ev = np.ascontiguousarray(events)
+    w = np.ascontiguousarray(weights, np.float32)
+    sn = np.ascontiguousarray(sens, np.float32)
+    cnt = np.zeros(4, np.int64)
+    rc = L.orc_hybrid_mlem(C.byref(s), _ptr(w), _ptr(sn), _ptr(ev), ev.shape[0], _ptr(rho),
+                           n_iterations, threads, _ptr(cnt))
+    if rc != 0:
+        raise MemoryError("orc_hybrid_mlem")
+    return rho, cnt

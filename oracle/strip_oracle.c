@@ -32,6 +32,7 @@ static int omp_get_thread_num(void) { return 0; }
 #define EXP expf
 #define ATAN atanf
 #include "strip_oracle_mlem.inc"
+#include "hybrid_oracle.inc"
 #undef REAL
 #undef SFX
 #undef SQRT

@@ -119,6 +119,68 @@ double orc_nll_grad(const orc_geom* g, double support_sigma_z, double support_si
                     double* grad_rho, double* grad_sigma, int n_threads,
                     int64_t* n_skipped);
 
+/* ---- 3D hybrid reconstruction (src/3d/hybrid/reconstruction.h) ----------------
+ * Float instantiation with S = short, one plane half (n_planes_half = 1) and the
+ * 2D sensitivity: the reference command's default flow (reconstruction_cmd.cpp:
+ * 463-544) without --sensitivity. */
+
+/* PET2D::LineSegment<float> fields in declaration order (line_segment.h:87-93). */
+typedef struct orc_segment {
+  float start_x, start_y, end_x, end_y, mid_x, mid_y, dir_x, dir_y, normal_x, normal_y;
+  float length, distance_from_origin;
+} orc_segment;
+
+/* PET2D::Pixel<short> (pixel.h:18). */
+typedef struct orc_pixel {
+  int16_t x, y;
+} orc_pixel;
+
+/* Hybrid Scanner::Response (3d/hybrid/scanner.h:71-76): LOR (first, second),
+ * z_up, z_dn, dl. */
+typedef struct orc_hybrid_response {
+  int16_t first, second;
+  float z_up, z_dn, dl;
+} orc_hybrid_response;
+
+/* Reconstruction::FrameEvent (reconstruction.h:53-63) with F = float, S = short
+ * and 64-bit size_t: the explicit pads are the compiler's alignment padding. */
+typedef struct orc_frame_event {
+  int16_t first, second;
+  float up, right, tan, sec;
+  uint32_t pad0;
+  uint64_t info_begin, info_end;
+  int16_t plane_begin, plane_end;
+  uint32_t pad1;
+} orc_frame_event;
+
+/* GeometrySOA arrays (2d/barrel/geometry_soa.h:268-283), the voxel grid
+ * (3d/geometry/voxel_grid.h:22-26 over pixel_grid.h:22-30) and the scanner
+ * quantities Reconstruction reads (sigma_z(), sigma_dl(), length). */
+typedef struct orc_hybrid {
+  int32_t n_detectors;          /* n_lors = (n + 1) n / 2 */
+  int64_t n_pixel_infos;
+  const orc_segment* segments;  /* [n_lors] */
+  const float* lor_widths;      /* [n_lors] */
+  const orc_pixel* pixels;      /* [n_pixel_infos] */
+  const float* positions;       /* [n_pixel_infos], ascending within each LOR */
+  const uint64_t* info_begin;   /* [n_lors] */
+  const uint64_t* info_end;     /* [n_lors] */
+  int32_t n_columns, n_rows, n_planes;
+  float pixel_size, lower_left_x, lower_left_y, z_left;
+  float sigma_z, sigma_dl, length;
+} orc_hybrid;
+
+void orc_hybrid_calculate_weight(const orc_hybrid* g, float* weights);
+void orc_hybrid_calculate_sensitivity(const orc_hybrid* g, const float* weights, float* sens);
+void orc_hybrid_normalize(const orc_hybrid* g, float* weights, const float* sens);
+int orc_hybrid_translate(const orc_hybrid* g, const orc_hybrid_response* r, const float* weights,
+                         orc_frame_event* e);
+int64_t orc_hybrid_translate_all(const orc_hybrid* g, const orc_hybrid_response* r, int64_t n,
+                                 const float* weights, orc_frame_event* out);
+int orc_hybrid_mlem(const orc_hybrid* g, const float* weights, const float* sens,
+                    const orc_frame_event* ev, int64_t n, float* rho, int n_iterations,
+                    int n_threads, int64_t* counters);
+
 #ifdef __cplusplus
 }
 #endif
