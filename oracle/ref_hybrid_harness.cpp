@@ -2,7 +2,7 @@
 // PET3D::Hybrid::Reconstruction<Scanner, PET2D::Strip::GaussianKernel<float>>
 // (src/3d/hybrid/reconstruction.h), instantiated from the reference headers and
 // driven the way 3d_hybrid_reconstruction drives it without --sensitivity
-// (src/3d/hybrid/reconstruction_cmd.cpp:463-544): calculate_weight (unless the
+// (src/3d/hybrid/reconstruction_cmd.cpp:462-541): calculate_weight (unless the
 // weights are given, as with --system), calculate_sensitivity or
 // set_sensitivity_to_one (--sens-to-one), normalize_geometry_weights, the
 // responses read through operator<< (translate_to_frame and the bounding-box

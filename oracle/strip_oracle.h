@@ -122,7 +122,7 @@ double orc_nll_grad(const orc_geom* g, double support_sigma_z, double support_si
 /* ---- 3D hybrid reconstruction (src/3d/hybrid/reconstruction.h) ----------------
  * Float instantiation with S = short, one plane half (n_planes_half = 1) and the
  * 2D sensitivity: the reference command's default flow (reconstruction_cmd.cpp:
- * 463-544) without --sensitivity. */
+ * 462-541) without --sensitivity. */
 
 /* PET2D::LineSegment<float> fields in declaration order (line_segment.h:87-93). */
 typedef struct orc_segment {
