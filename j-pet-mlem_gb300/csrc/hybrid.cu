@@ -14,14 +14,14 @@
 // runs in memory; the reference's plane-major order (voxel_grid.h:54-56) is used
 // only at the boundary (set_image / get_image).
 //
-// Iteration kernel: one warp per event.  The event's pixel infos are taken in
-// chunks of kPix; for each chunk the lanes compute the per-pixel constants of
-// the strip kernel (the terms that do not depend on z) into shared memory, then
-// walk the chunk's pixel x plane voxels flattened, 32 consecutive voxels per
-// step, so that lanes on one pixel touch consecutive planes.  The voxel's weight
-// K(z, up) w_pixel rho is kept in a per-lane shared-memory cache (the first
-// kCache steps) for the back-projection, which adds weight / denominator with
-// one global float atomic per voxel.
+// Iteration kernel: one CTA per event.  The threads compute the event's
+// per-pixel constants of the strip kernel (the terms that do not depend on z)
+// into shared memory, then walk the pixel-info x plane voxels flattened, one
+// CTA-wide step of consecutive voxels at a time, so that neighbouring threads
+// touch neighbouring planes of one pixel.  Each thread keeps the weights
+// K(z, up) w_pixel rho of its first voxels in shared memory for the
+// back-projection, which adds weight / denominator with one global float
+// atomic per voxel; the denominator is reduced across the CTA.
 #include <cuda_runtime.h>
 
 #include <cub/device/device_radix_sort.cuh>
@@ -70,22 +70,24 @@ struct HybConst {
   float ps, z_left;     // voxel size, VoxelGrid::z_left
   float llcx, llcy;     // PixelGrid::lower_left_center
   float L2;             // length / 2 (GaussianKernel::sensitivity)
+  float exp_bpq;        // -log2(e) / sigma_z^2: exponent coefficient of (dz - dy tan)^2
   int32_t n_columns, n_rows, n_planes;
   int32_t n_lors;
   int64_t n_infos;
 };
 
-constexpr int kPix = 128;     // pixel infos per chunk
-constexpr int kCache = 64;    // cached voxel steps per lane (kCache * 32 voxels per event)
-constexpr int kWarps = 4;     // warps per CTA of the iteration kernel
+// Sizes of the iteration kernel (compile-time; -D overrides for tuning sweeps).
+#ifndef JPET_HYBRID_THREADS
+#define JPET_HYBRID_THREADS 128
+#endif
+#ifndef JPET_HYBRID_CACHE_STEPS
+#define JPET_HYBRID_CACHE_STEPS 32
+#endif
+constexpr int kThreads = JPET_HYBRID_THREADS;     // CTA size: one event per CTA at a time
+constexpr int kSteps = JPET_HYBRID_CACHE_STEPS;   // voxel weights a thread keeps for the back-projection
+constexpr int kPix = 256;                         // pixel infos per chunk
+constexpr int kWarpsPerCta = kThreads / 32;
 constexpr float kPi = 3.14159265358979323846f;
-
-// Per-warp shared memory of the iteration kernel.
-struct WarpSmem {
-  float4 pa[kPix];  // dy, element_before_exp, (r ipd r), pixel weight
-  float4 pb[kPix];  // 1/(R - up), 1/(R + up), sensitivity, base index (int bits)
-  float cache[kCache * 32];
-};
 
 __device__ __forceinline__ int64_t lor_index(int16_t first, int16_t second) {
   return static_cast<int64_t>(static_cast<int32_t>(first) * (first + 1) / 2 + second);
@@ -361,6 +363,7 @@ __global__ void to_reference_layout(const float* __restrict__ in, float* __restr
 
 struct EvC {
   float up, right, tan, sec, R;
+  float z0;  // centre of the event's first plane (voxel_grid.h:40-42)
   int32_t plane_begin;
 };
 
@@ -368,6 +371,13 @@ struct EvC {
 __device__ __forceinline__ float ex2(float x) {
   float y;
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// rcp.approx of the hardware (relative error below 2^-23).
+__device__ __forceinline__ float rcp(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 
@@ -397,45 +407,107 @@ __device__ __forceinline__ void pixel_terms(const HybConst& c, const EvC& e, flo
   const float br = __fmul_rn(__fmul_rn(-2.0f, dy), e.sec);
   const float brr = __fmul_rn(__fmul_rn(br, c.ipd), br);
   const int pix = x + c.n_columns * y;
-  pa = make_float4(dy, ebe, brr, w[i]);
+  // the exponent's z-independent part -log2(e) (r ipd r) / 2 and the pixel
+  // weight times pi (the frame sensitivity's 1/pi) are folded in here
+  pa = make_float4(dy, ebe, brr * (-0.5f * 1.4426950408889634f), w[i] * kPi);
   pb = make_float4(__frcp_rn(__fsub_rn(e.R, up)), __frcp_rn(__fadd_rn(e.R, up)), sens[pix],
                    __int_as_float(pix * c.n_planes));
 }
 
-// weight = GaussianKernel::normalized(...) * pixel weight * rho of voxel
-// (pixel, plane iz), reconstruction.h:327-363.  The frame sensitivity's
-// atan(a) - atan(b) is evaluated as atan2(a - b, 1 + a b), the same angle.
-__device__ __forceinline__ float voxel_weight(const HybConst& c, const EvC& e, const float4 pa,
-                                              const float4 pb, int iz,
-                                              const float* __restrict__ rho) {
-  const float z = __fadd_rn(__fmul_rn(__fadd_rn(static_cast<float>(iz), 0.5f), c.ps), c.z_left);
-  const float dz = z - e.right;
-  const float bpq = fmaf(-pa.x, e.tan, dz);
-  const float half = bpq * c.ipz * bpq;
-  const float b = fmaf(2.0f, half, pa.z);
-  const float K = pa.y * ex2(b * (-0.5f * 1.4426950408889634f));
-  const float lp = c.L2 + z, lm = c.L2 - z;
-  const float a = fminf(lm * pb.x, lp * pb.y);
-  const float bb = fmaxf(-lp * pb.x, -lm * pb.y);
-  const float ang = atan2f(a - bb, fmaf(a, bb, 1.0f));
-  const float kernel2d = __fdividef(K * kPi, ang);
-  if (kernel2d <= 0.0f) return 0.0f;
-  return kernel2d * pa.w * __ldg(&rho[__float_as_int(pb.w) + iz]);
+// Arctangent of y / x in (-pi, pi]: reduction to r = min(|x|, |y|) / max(|x|, |y|)
+// in [0, 1], atan(r) = r P(r^2) with P of degree 8 fitted by csrc/fit_atan.py
+// (maximum absolute error 1e-7 on [0, 1] in float arithmetic), then the
+// octant and sign reflections.  Branch-free.
+__device__ __forceinline__ float atan2_poly(float y, float x) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float r = fminf(ax, ay) * rcp(fmaxf(ax, ay));
+  const float s = r * r;
+  float p = 2.456588438e-03f;
+  p = fmaf(p, s, -1.440078672e-02f);
+  p = fmaf(p, s, 3.978023678e-02f);
+  p = fmaf(p, s, -7.234767079e-02f);
+  p = fmaf(p, s, 1.049889922e-01f);
+  p = fmaf(p, s, -1.416121572e-01f);
+  p = fmaf(p, s, 1.998590529e-01f);
+  p = fmaf(p, s, -3.333259821e-01f);
+  p = fmaf(p, s, 9.999998808e-01f);
+  p *= r;
+  p = (ay > ax) ? 1.57079632679489662f - p : p;
+  p = (x < 0.0f) ? kPi - p : p;
+  return copysignf(p, y);
 }
 
-__global__ void __launch_bounds__(kWarps * 32)
+// weight = GaussianKernel::normalized(...) * pixel weight * rho of voxel
+// (pixel, plane col), reconstruction.h:327-363, with the plane's terms
+// dz = z - right, lp = L/2 + z, lm = L/2 - z.  exp(-b_ic_b / 2) is
+// 2^(exp_bpq (dz - dy tan)^2 + pa.z); the frame sensitivity's
+// atan(a) - atan(b) (gaussian_kernel.h:140-150) is evaluated as
+// atan2(a - b, 1 + a b), the same angle for every a, b; a non-positive kernel
+// value gives weight 0 as in the reference (reconstruction.h:335-341).
+__device__ __forceinline__ float plane_weight(const HybConst& c, const EvC& e, const float4 pa,
+                                              const float4 pb, float dz, float lp, float lm,
+                                              int col, const float* __restrict__ rho) {
+  const float bpq = fmaf(-pa.x, e.tan, dz);
+  const float K = pa.y * ex2(fmaf(bpq * bpq, c.exp_bpq, pa.z));
+  const float a = fminf(lm * pb.x, lp * pb.y);
+  const float bb = fmaxf(-lp * pb.x, -lm * pb.y);
+  const float ang = atan2_poly(a - bb, fmaf(a, bb, 1.0f));
+  const float v = (K * pa.w) * rcp(ang) * __ldg(&rho[__float_as_int(pb.w) + col]);
+  return ang < 0.0f ? 0.0f : v;
+}
+
+// The same for the event's k-th plane, z = z0 + k pixel_size.
+__device__ __forceinline__ float voxel_weight(const HybConst& c, const EvC& e, const float4 pa,
+                                              const float4 pb, int k,
+                                              const float* __restrict__ rho) {
+  const float z = fmaf(static_cast<float>(k), c.ps, e.z0);
+  return plane_weight(c, e, pa, pb, z - e.right, c.L2 + z, c.L2 - z, e.plane_begin + k, rho);
+}
+
+// Advances a thread's (pixel, plane) position by one CTA-wide step of the
+// flattened walk: kThreads voxels = q pixels and r planes.
+__device__ __forceinline__ void walk(int& i, int& k, int q, int r, int npl) {
+  k += r;
+  i += q;
+  if (k >= npl) {
+    k -= npl;
+    ++i;
+  }
+}
+
+// Multiplicity of info i's voxels in the back-projection.  The reference keeps
+// the kernel values in a voxel-indexed image (reconstruction.h:339,361,368)
+// and back-projects every occurrence of a voxel with the value written last.
+// Pixels of one LOR are distinct, so the only repeated pixel is the info one
+// past the LOR's end that the range takes in (reconstruction.h:134-140): when
+// it repeats the pixel of info dup, info dup contributes nothing and the last
+// info twice.
+__device__ __forceinline__ float multiplicity(int64_t i, int dup, int64_t last) {
+  return dup < 0 ? 1.0f : (i == dup ? 0.0f : (i == last ? 2.0f : 1.0f));
+}
+
+// One CTA per event.  The pixel terms of up to kPix infos go to shared
+// memory.  Thread tid takes plane tid % npl of the pixels tid / npl,
+// tid / npl + G, ... (G = kThreads / npl groups), so neighbouring threads touch
+// neighbouring planes of one pixel and every z-dependent term is computed once
+// per event; each thread keeps its first kSteps weights in shared memory for
+// the back-projection.  Events with more than kPix infos or kThreads planes are
+// walked flattened, chunk by chunk, and recomputed in the back-projection.
+__global__ void __launch_bounds__(kThreads)
     iterate_kernel(const jpet_hybrid_frame_event* __restrict__ ev, int64_t n,
                    const float4* __restrict__ seg, const int16_t* __restrict__ p16,
                    const float* __restrict__ w, const float* __restrict__ sens,
                    const float* __restrict__ rho, float* __restrict__ out, HybConst c,
                    unsigned long long* __restrict__ n_positive) {
-  extern __shared__ float4 smem_raw[];
-  const int lane = threadIdx.x & 31;
-  const int wid = threadIdx.x >> 5;
-  WarpSmem& sm = reinterpret_cast<WarpSmem*>(smem_raw)[wid];
-  const int64_t n_warps = static_cast<int64_t>(gridDim.x) * kWarps;
+  __shared__ float4 pa[kPix];  // dy, element_before_exp, exponent term, pixel weight * pi
+  __shared__ float4 pb[kPix];  // 1/(R - up), 1/(R + up), sensitivity, base index (int bits)
+  __shared__ float cache[kSteps * kThreads];  // weights of each thread's first kSteps voxels
+  __shared__ float red_den[kWarpsPerCta];
+  __shared__ int red_dup[kWarpsPerCta];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const uint32_t* p32 = reinterpret_cast<const uint32_t*>(p16);
   unsigned long long positive = 0;
-  for (int64_t ei = static_cast<int64_t>(blockIdx.x) * kWarps + wid; ei < n; ei += n_warps) {
+  for (int64_t ei = blockIdx.x; ei < n; ei += gridDim.x) {
     const jpet_hybrid_frame_event fe = ev[ei];
     const int npl = fe.plane_end - fe.plane_begin;
     const int64_t nin = static_cast<int64_t>(fe.pixel_info_end - fe.pixel_info_begin);
@@ -449,85 +521,127 @@ __global__ void __launch_bounds__(kWarps * 32)
     e.sec = fe.sec;
     e.R = __fdiv_rn(seg[3 * l + 2].z, 2.0f);
     e.plane_begin = fe.plane_begin;
-    // flattened (pixel, plane) walk: lane starts at (lane / npl, lane % npl)
-    // and advances by 32 voxels = q pixels and r planes per step
-    const int q = 32 / npl, r = 32 - q * npl;
-    const int i0 = lane / npl, k0 = lane - i0 * npl;
-    // The reference keeps the kernel values in a voxel-indexed image
-    // (reconstruction.h:339,361,368) and back-projects every occurrence of a
-    // voxel with the value written last.  Pixels of one LOR are distinct, so
-    // the only repeated pixel is the info one past the LOR's end that the
-    // range takes in (reconstruction.h:134-140): when it repeats an earlier
-    // info's pixel, that earlier info contributes nothing and the last info
-    // twice.
-    const uint32_t last_pixel = reinterpret_cast<const uint32_t*>(p16)[fe.pixel_info_end - 1];
-    int64_t dup = -1;
+    e.z0 = __fadd_rn(__fmul_rn(__fadd_rn(static_cast<float>(fe.plane_begin), 0.5f), c.ps),
+                     c.z_left);
+    const uint32_t last_pixel = p32[fe.pixel_info_end - 1];
+    // main path: at most kPix infos and kThreads planes; thread tid holds
+    // plane k of pixel group g (G groups of npl threads)
+    const bool one_chunk = nin <= kPix && npl <= kThreads;
+    const int G = one_chunk ? kThreads / npl : 1;
+    const int g0 = tid / npl, kk = tid - g0 * npl;
+    const bool active = g0 < G;
+    const int col = e.plane_begin + kk;
+    const float z = fmaf(static_cast<float>(kk), c.ps, e.z0);
+    const float dz = z - e.right, lp = c.L2 + z, lm = c.L2 - z;
+    // fallback: the flattened walk, kThreads voxels = q pixels and r planes per step
+    const int q = kThreads / npl, r = kThreads - q * npl;
+    const int i0 = g0, k0 = kk;
+    int dup = -1;  // info whose pixel the range's last info repeats (-1: none)
     float den = 0.0f;
-    int slot = 0;
-    for (int64_t cb = 0; cb < nin; cb += kPix) {
-      const int cn = static_cast<int>(nin - cb < kPix ? nin - cb : kPix);
-      __syncwarp();
-      for (int j = lane; j < cn; j += 32) {
-        const int64_t info = static_cast<int64_t>(fe.pixel_info_begin) + cb + j;
-        pixel_terms(c, e, s1, p16, w, sens, info, sm.pa[j], sm.pb[j]);
-        if (cb + j < nin - 1 && reinterpret_cast<const uint32_t*>(p16)[info] == last_pixel)
-          dup = cb + j;
+    if (one_chunk) {
+      const int ni = static_cast<int>(nin);
+      __syncthreads();
+      for (int j = tid; j < ni; j += kThreads) {
+        const int64_t info = static_cast<int64_t>(fe.pixel_info_begin) + j;
+        pixel_terms(c, e, s1, p16, w, sens, info, pa[j], pb[j]);
+        if (j < ni - 1 && p32[info] == last_pixel) dup = j;
       }
-      __syncwarp();
-      int i = i0, k = k0;
-      while (i < cn) {
-        const float v = voxel_weight(c, e, sm.pa[i], sm.pb[i], e.plane_begin + k, rho);
-        den = fmaf(v, sm.pb[i].z, den);
-        if (slot < kCache) sm.cache[slot * 32 + lane] = v;
-        ++slot;
-        k += r;
-        i += q;
-        if (k >= npl) {
-          k -= npl;
-          ++i;
+      __syncthreads();
+      // thread = (pixel group g, plane k): groups walk the pixels g, g + G, ...;
+      // the first kSteps weights are kept for the back-projection
+      const int nmine = active ? (ni - g0 + G - 1) / G : 0;  // pixels of this thread
+      const int ncached = nmine < kSteps ? nmine : kSteps;
+      const float4* a = pa + g0;
+      const float4* b = pb + g0;
+      float* cp = cache + tid;
+      for (int t = 0; t < ncached; ++t, a += G, b += G, cp += kThreads) {
+        const float4 bv = *b;
+        const float v = plane_weight(c, e, *a, bv, dz, lp, lm, col, rho);
+        den = fmaf(v, bv.z, den);
+        *cp = v;
+      }
+      for (int t = ncached; t < nmine; ++t, a += G, b += G) {
+        const float4 bv = *b;
+        den = fmaf(plane_weight(c, e, *a, bv, dz, lp, lm, col, rho), bv.z, den);
+      }
+    } else {
+      for (int64_t cb = 0; cb < nin; cb += kPix) {
+        const int cn = static_cast<int>(nin - cb < kPix ? nin - cb : kPix);
+        __syncthreads();
+        for (int j = tid; j < cn; j += kThreads) {
+          const int64_t info = static_cast<int64_t>(fe.pixel_info_begin) + cb + j;
+          pixel_terms(c, e, s1, p16, w, sens, info, pa[j], pb[j]);
+          if (cb + j < nin - 1 && p32[info] == last_pixel) dup = static_cast<int>(cb + j);
         }
+        __syncthreads();
+        for (int i = i0, k = k0; i < cn; walk(i, k, q, r, npl))
+          den = fmaf(voxel_weight(c, e, pa[i], pb[i], k, rho), pb[i].z, den);
       }
     }
     for (int o = 16; o > 0; o >>= 1) {
       den += __shfl_xor_sync(0xffffffffu, den, o);
-      dup = max(dup, static_cast<int64_t>(__shfl_xor_sync(0xffffffffu, static_cast<long long>(dup), o)));
+      dup = max(dup, __shfl_xor_sync(0xffffffffu, dup, o));
+    }
+    if (lane == 0) {
+      red_den[wid] = den;
+      red_dup[wid] = dup;
+    }
+    __syncthreads();
+    den = 0.0f;
+    dup = -1;
+#pragma unroll
+    for (int j = 0; j < kWarpsPerCta; ++j) {
+      den += red_den[j];
+      dup = max(dup, red_dup[j]);
     }
     if (!(den > 0.0f)) continue;
-    positive += (lane == 0);
+    positive += (tid == 0);
     const float inv = __frcp_rn(den);
-    slot = 0;
-    for (int64_t cb = 0; cb < nin; cb += kPix) {
-      const int cn = static_cast<int>(nin - cb < kPix ? nin - cb : kPix);
-      if (nin > kPix) {
-        // the chunk's pixel terms were overwritten by a later chunk
-        __syncwarp();
-        for (int j = lane; j < cn; j += 32)
-          pixel_terms(c, e, s1, p16, w, sens, fe.pixel_info_begin + cb + j, sm.pa[j], sm.pb[j]);
-        __syncwarp();
+    if (one_chunk) {
+      const int ni = static_cast<int>(nin);
+      const int nmine = active ? (ni - g0 + G - 1) / G : 0;
+      const int ncached = nmine < kSteps ? nmine : kSteps;
+      const float4* a = pa + g0;
+      const float4* b = pb + g0;
+      const float* cp = cache + tid;
+      float* o = out + col;
+      if (dup < 0) {
+        int t = 0;
+        for (; t < ncached; ++t, b += G, cp += kThreads) {
+          const float v = *cp;
+          if (v != 0.0f) atomicAdd(o + __float_as_int(b->w), v * inv);
+        }
+        for (a += t * G; t < nmine; ++t, a += G, b += G) {
+          const float4 bv = *b;
+          const float v = plane_weight(c, e, *a, bv, dz, lp, lm, col, rho);
+          if (v != 0.0f) atomicAdd(o + __float_as_int(bv.w), v * inv);
+        }
+      } else {
+        for (int t = 0, i = g0; t < nmine; ++t, i += G, a += G, b += G, cp += kThreads) {
+          const float4 bv = *b;
+          const float v = t < ncached ? *cp : plane_weight(c, e, *a, bv, dz, lp, lm, col, rho);
+          const float x = v * multiplicity(i, dup, ni - 1);
+          if (x != 0.0f) atomicAdd(o + __float_as_int(bv.w), x * inv);
+        }
       }
-      int i = i0, k = k0;
-      while (i < cn) {
-        const int iz = e.plane_begin + k;
-        const float v = slot < kCache ? sm.cache[slot * 32 + lane]
-                                      : voxel_weight(c, e, sm.pa[i], sm.pb[i], iz, rho);
-        ++slot;
-        const int64_t info = cb + i;
-        const float m = (dup < 0) ? 1.0f : (info == dup ? 0.0f : (info == nin - 1 ? 2.0f : 1.0f));
-        if (v != 0.0f && m != 0.0f)
-          atomicAdd(&out[__float_as_int(sm.pb[i].w) + iz], (v * m) * inv);
-        k += r;
-        i += q;
-        if (k >= npl) {
-          k -= npl;
-          ++i;
+    } else {
+      for (int64_t cb = 0; cb < nin; cb += kPix) {
+        const int cn = static_cast<int>(nin - cb < kPix ? nin - cb : kPix);
+        __syncthreads();
+        for (int j = tid; j < cn; j += kThreads)
+          pixel_terms(c, e, s1, p16, w, sens, static_cast<int64_t>(fe.pixel_info_begin) + cb + j,
+                      pa[j], pb[j]);
+        __syncthreads();
+        for (int i = i0, k = k0; i < cn; walk(i, k, q, r, npl)) {
+          const float x = voxel_weight(c, e, pa[i], pb[i], k, rho) * multiplicity(cb + i, dup, nin - 1);
+          if (x != 0.0f) atomicAdd(&out[__float_as_int(pb[i].w) + e.plane_begin + k], x * inv);
         }
       }
     }
   }
-  if (lane == 0 && positive) atomicAdd(n_positive, positive);
+  if (tid == 0 && positive) atomicAdd(n_positive, positive);
 }
 
-constexpr size_t kSmemPerCta = sizeof(WarpSmem) * kWarps;
 
 }  // namespace
 
@@ -594,6 +708,7 @@ HybConst make_const(const jpet_hybrid_geom& g) {
   c.llcx = g.lower_left_x + g.pixel_size / 2.0f;
   c.llcy = g.lower_left_y + g.pixel_size / 2.0f;
   c.L2 = g.length / 2.0f;
+  c.exp_bpq = static_cast<float>(-1.4426950408889634 * static_cast<double>(c.ipz));
   c.n_columns = g.n_columns;
   c.n_rows = g.n_rows;
   c.n_planes = g.n_planes;
@@ -818,12 +933,8 @@ int jpet_hybrid_create(const jpet_hybrid_geom* g, const jpet_hybrid_opts* opts_i
               "device attribute");
   CREATE_CUDA(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "stream");
   h->stream = h->own_stream;
-  CREATE_CUDA(cudaFuncSetAttribute(iterate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(kSmemPerCta)),
-              "kernel attribute");
   int per_sm = 0;
-  CREATE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, iterate_kernel, kWarps * 32,
-                                                            kSmemPerCta),
+  CREATE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, iterate_kernel, kThreads, 0),
               "occupancy");
   h->iterate_blocks = std::max(1, per_sm) * h->n_sms;
 
@@ -1026,7 +1137,7 @@ int jpet_hybrid_iterate(jpet_hybrid_t* h, int n) {
     HYB_CUDA(h, cudaMemsetAsync(h->counters.p + 2, 0, sizeof(unsigned long long), h->stream),
              "memset");
     if (h->n_events > 0) {
-      iterate_kernel<<<h->iterate_blocks, kWarps * 32, kSmemPerCta, h->stream>>>(
+      iterate_kernel<<<h->iterate_blocks, kThreads, 0, h->stream>>>(
           h->ev.p, h->n_events, h->seg.p, h->pix.p, h->w.p, h->sens.p, h->rho.p, h->out.p, h->c,
           h->counters.p + 2);
       HYB_CUDA(h, cudaGetLastError(), "iterate");
