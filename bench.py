@@ -74,6 +74,11 @@ def parse():
     p.add_argument("--adjoint-report", action="store_true",
                    help="the adjoint entry alone (loss + gradient timing, no calibration)")
     p.add_argument("--adjoint-events", type=int, default=5_000_000)
+    p.add_argument("--no-hybrid", action="store_true",
+                   help="skip the 3D hybrid entry (384-detector ring, 200x200x125 voxels)")
+    p.add_argument("--hybrid-events", type=int, default=10_000_000)
+    p.add_argument("--hybrid-report", action="store_true",
+                   help="the 3D hybrid entry alone")
     p.add_argument("--precision-report", action="store_true",
                    help="print the precision-stress comparison instead of the headline line")
     p.add_argument("--variant", type=int, default=0,
@@ -363,6 +368,13 @@ def gb300_arm(args, wl, world, rank, local):
             adjoint = adjoint_summary(local, ex2_peak=(peaks or {}).get("ex2_per_s"))
         except Exception as exc:  # reported, the headline line still prints
             adjoint = {"error": f"{type(exc).__name__}: {exc}"}
+    hybrid = None
+    if not args.no_hybrid:
+        try:
+            hybrid = hybrid_summary(local, args.hybrid_events,
+                                    sm_mhz=(clk or {}).get("sm_mhz"))
+        except Exception as exc:  # reported, the headline line still prints
+            hybrid = {"error": f"{type(exc).__name__}: {exc}"}
     hbm, hbm_kind = hbm_peak()
     roofline = None
     if peaks:
@@ -429,6 +441,7 @@ def gb300_arm(args, wl, world, rank, local):
         "kernel_ms_per_iteration": kernel_ms,
         "batched": batched,
         "adjoint": adjoint,
+        "hybrid": hybrid,
     }
     print(json.dumps(line), flush=True)
 
@@ -646,14 +659,15 @@ def profile_traffic(n_events, key="dram_bytes_per_launch", variant=0):
     variant runs (dram__bytes_read.sum + dram__bytes_write.sum,
     smsp__inst_executed.sum of one launch), scaled from the captured event count
     to n_events."""
-    name = {0: "iterate_union_traffic.json", 3: "iterate_rows_traffic.json"}.get(variant)
+    name = {0: "iterate_union_traffic.json", 3: "iterate_rows_traffic.json",
+            "hybrid": "hybrid_iterate_traffic.json"}.get(variant)
     if name is None:
         return None
     path = os.path.join(ROOT, "profiles", name)
     try:
         with open(path) as f:
             d = json.load(f)
-        return d[key] * n_events / d["events"]
+        return d[key] * n_events / d.get("units", d.get("events"))
     except (OSError, KeyError, ValueError, ZeroDivisionError):
         return None
 
@@ -801,6 +815,121 @@ def adjoint_summary(local, n_events=5_000_000, ex2_peak=None, calibrate=True):
     return out
 
 
+def hybrid_summary(local, n_events=10_000_000, steps=5, warmup=2, cpu_seconds=10.0,
+                   iterations=10, sm_mhz=None):
+    """The 3D hybrid reconstruction (include/jpet_hybrid.h) on the "hybrid-384"
+    configuration: a 384-detector ring of radius 430 mm, 200 x 200 pixels of
+    4 mm and 125 planes, sigma_z / sigma_dl 15 / 60 mm (3d_hybrid_reconstruction's
+    defaults), n_events responses of a seeded 3D ellipsoid phantom.
+      value   event-iterations/s with the frame events resident on the device
+              (CUDA events around `steps` iterations on the handle's stream)
+      e2e     host responses -> set_responses (frame events and the filter on
+              the device) -> uniform image -> `iterations` iterations -> image
+              back to the host, through the C ABI
+      cpu_baseline  the CPU restatement (release build, all host threads) on
+              a prefix of the same frame events, one iteration
+      parity  one iteration of that prefix on the GPU against the restatement"""
+    import numpy as np
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from jpet_strip import hybrid as HY
+    from jpet_strip import hybrid_workloads as H
+
+    t0 = time.perf_counter()
+    g, _, _ = H.workload("hybrid-384")
+    resp = H.responses(g, n_events, seed=3)
+    gen_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream(device=local)
+    with HY.HybridReconstruction(g, device=local) as r:
+        r.set_stream(stream.cuda_stream)
+        t0 = time.perf_counter()
+        r << resp
+        r.synchronize()
+        set_s = time.perf_counter() - t0
+        st = r.statistics()
+        for _ in range(warmup):
+            r(1)
+        r.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        r(steps)
+        b.record(stream)
+        b.synchronize()
+        ms = a.elapsed_time(b) / steps
+        kept = r.n_events
+        frames = r.frame_events()
+        # end to end through the C ABI: host responses in, image out
+        pinned = np.empty_like(resp)
+        pinned[:] = resp
+        ones = np.ones(g.n_voxels, np.float32)
+        e2e = []
+        for k in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r << pinned
+            r.rho = ones
+            r(iterations)
+            img = r.rho
+            if k:
+                e2e.append(time.perf_counter() - t0)
+        del img
+    voxels = st["used_voxels"]
+    out = {"workload": "hybrid-384", "detectors": g.n_detectors, "grid": "200x200x125",
+           "voxel_mm": 4.0, "sigma_z_mm": 15.0, "sigma_dl_mm": 60.0,
+           "pixel_infos": g.n_pixel_infos, "responses": n_events, "events_kept": kept,
+           "voxels_per_iteration": voxels, "voxels_per_event": voxels / max(kept, 1),
+           "ms_per_iteration": ms, "value": kept / (ms * 1e-3),
+           "unit": "event-iterations/s", "voxel_evals_per_s": voxels / (ms * 1e-3),
+           "generate_seconds": gen_s, "set_responses_seconds": set_s,
+           "e2e": {"value": kept * iterations / e2e[0], "unit": "event-iterations/s",
+                   "iterations_per_step": iterations, "seconds_per_step": e2e[0],
+                   "h2d_bytes_per_step": int(resp.nbytes + 4 * g.n_voxels),
+                   "d2h_bytes_per_step": int(4 * g.n_voxels)}}
+    prof = profile_traffic(voxels, "warp_instructions_per_launch", variant="hybrid")
+    if prof:
+        # instruction-issue bound: 4 schedulers per SM issue one warp instruction
+        # per clock each; the count is the committed capture's, scaled by voxels
+        n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+        out["roofline"] = {"bound": "issue", "unit": "warp instructions/s",
+                           "warp_instructions_per_launch": prof,
+                           "achieved": prof / (ms * 1e-3),
+                           "traffic": profile_traffic(voxels, variant="hybrid")}
+        if sm_mhz:
+            peak = 4 * n_sm * sm_mhz * 1e6
+            out["roofline"].update({"peak": peak, "frac": prof / (ms * 1e-3) / peak,
+                                    "sm_mhz": sm_mhz})
+    # CPU baseline and parity on a prefix of the same frame events
+    w, s = O.hybrid_setup(g)
+    threads = os.cpu_count() or 1
+    n = 2000
+    dt = 0.0
+    while True:
+        t0 = time.perf_counter()
+        want, cnt = O.hybrid_mlem(g, w, s, frames[:n], 1, threads=threads, release=True)
+        dt = time.perf_counter() - t0
+        if dt > cpu_seconds / 4 or n >= kept:
+            break
+        n = min(kept, int(n * max(2.0, cpu_seconds / 4 / max(dt, 1e-3))))
+    cpu_rate = n / dt
+    out["cpu_baseline"] = {"value": cpu_rate, "unit": "event-iterations/s", "cores": threads,
+                           "kind": "port",
+                           "build": "oracle/liboracle_strip_release.so (-O3, OpenMP, FMA "
+                                    "contraction)",
+                           "sample": f"first {n} of the {kept} frame events, one iteration "
+                                     f"from a uniform image",
+                           "voxel_evals_per_s": float(cnt[2]) / dt}
+    with HY.HybridReconstruction(g, device=local) as r:
+        r.set_frame_events(frames[:n])
+        r(1)
+        got = r.rho
+    out["parity"] = {"events": n, "rel_l2_vs_oracle_1_iteration": _rel(got, want)}
+    out["speedup_vs_cpu_baseline"] = out["value"] / cpu_rate
+    return out
+
+
 def precision_report(args, local):
     """Precision stress: the 1 mm lesion workload in every accumulation mode.
     Full scale: time per iteration and each image against the reference
@@ -892,6 +1021,8 @@ def main():
         accuracy_full_report(args, wl, local)
     elif args.calibration_report:
         calibration_report(local)
+    elif args.hybrid_report:
+        print(json.dumps({"hybrid": hybrid_summary(local, args.hybrid_events)}), flush=True)
     elif args.adjoint_report:
         print(json.dumps({"adjoint": adjoint_summary(local, args.adjoint_events,
                                                      calibrate=False)}), flush=True)

@@ -269,8 +269,8 @@ class OrcHybrid(C.Structure):
     ]
 
 
-def _hyb_lib():
-    L = lib()
+def _hyb_lib(release: bool = False):
+    L = lib(release)
     if not hasattr(L, "_hyb_ready"):
         hp = C.POINTER(OrcHybrid)
         vp = C.c_void_p
@@ -334,10 +334,12 @@ def _frame_dtype():
         "itemsize": 48})
 
 
-def hybrid_mlem(g, weights, sens, events, n_iterations: int, rho=None, threads: int = 1):
+def hybrid_mlem(g, weights, sens, events, n_iterations: int, rho=None, threads: int = 1,
+                release: bool = False):
     """n_iterations of Reconstruction::operator(); returns (rho float32[n_voxels],
-    counters int64[4]: used_events, used_pixels, used_voxels, positive denominators)."""
-    L = _hyb_lib()
+    counters int64[4]: used_events, used_pixels, used_voxels, positive denominators).
+    release=True runs the timing build (FMA contraction allowed)."""
+    L = _hyb_lib(release)
     s, keep = hybrid_struct(g)
     rho = (np.ones(g.n_voxels, np.float32) if rho is None
            else np.array(rho, np.float32, copy=True).reshape(-1))
