@@ -19,6 +19,13 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return y;
 }
 
+// 1/x within one ulp (subnormal inputs are not flushed to zero)
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ float lg2_approx(float x) {
   float y;
   asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));

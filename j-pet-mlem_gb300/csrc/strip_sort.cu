@@ -3,11 +3,16 @@
 //
 // Key, most significant first: the image tile of the box's top-left corner
 // (the tile kernels' work unit; oversize boxes and empty boxes get two keys past
-// the last tile, so they end up behind the tile events, in that order); the
-// corner's row and column inside the tile; tan quantised to 12 bits.  Within a
-// tile, consecutive events then have nearly the same box and in-ellipse rows,
-// which the batch-union kernel (strip_union.cu) relies on; the order is
-// deterministic (the sort is stable and the input order is the caller's).
+// the last tile, so they end up behind the tile events, in that order); tan in
+// buckets of 1/8; the corner's row and column inside the tile; tan quantised to
+// 12 bits.  Within a tile, consecutive events then have nearly the same box,
+// slope and in-ellipse rows, which the batch-union kernel (strip_union.cu)
+// relies on: its batches of similar events share one lane-to-pixel map, and a
+// batch's per-row union is widest where its events' slopes differ (at the box's
+// top and bottom rows).  Bucketing tan ahead of the corner trades about one
+// pixel of corner spread for a much narrower slope spread where few events share
+// a corner pixel.  The order is deterministic (the sort is stable and the input
+// order is the caller's).
 #include <cuda_runtime.h>
 
 #include <cub/cub.cuh>
@@ -27,7 +32,7 @@ __global__ void sort_keys_kernel(Tiling t, int64_t n, const float4* __restrict__
   const short4 b = ev_box[i];
   const int bw = b.z - b.x, bh = b.w - b.y;
   const uint64_t n_tiles = static_cast<uint64_t>(t.n_tiles_x) * static_cast<uint64_t>(t.n_tiles_y);
-  uint64_t tile, ry = 0, rx = 0, tq = 0;
+  uint64_t tile, ry = 0, rx = 0, tq = 0, tb = 0;
   if (bw <= 0 || bh <= 0) {
     tile = n_tiles + 1;
   } else if (bw > t.max_box_w || bh > t.max_box_h) {
@@ -39,8 +44,9 @@ __global__ void sort_keys_kernel(Tiling t, int64_t n, const float4* __restrict__
     // fminf/fmaxf drop a NaN operand, so every tan maps into [0, 4095]
     const float q = fminf(fmaxf((ev_geom[i].z + 4.0f) * 512.0f, 0.0f), 4095.0f);
     tq = static_cast<uint64_t>(q);
+    tb = tq >> 6;
   }
-  keys[i] = (tile << 28) | (ry << 20) | (rx << 12) | tq;
+  keys[i] = (tile << 34) | (tb << 28) | (ry << 20) | (rx << 12) | tq;
   idx[i] = static_cast<int32_t>(i);
 }
 
@@ -67,8 +73,8 @@ __global__ void gather_events_kernel(int64_t n_tile_events, int64_t n_over,
 int key_bits(const Tiling& t) {
   const uint64_t top = static_cast<uint64_t>(t.n_tiles_x) * static_cast<uint64_t>(t.n_tiles_y) + 1;
   int bits = 1;
-  while (bits < 36 && (top >> bits) != 0) ++bits;
-  return 28 + bits;
+  while (bits < 30 && (top >> bits) != 0) ++bits;
+  return 34 + bits;
 }
 
 }  // namespace

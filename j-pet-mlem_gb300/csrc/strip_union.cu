@@ -1,9 +1,9 @@
 // Batch-union MLEM iteration kernel for the CPU-reference semantics (the
 // default FP32 kernel), and the set-up passes that feed it.
 //
-// Events are sorted by image tile, then by their box corner inside the tile and
-// by tan (strip_sort.cu), so neighbouring events in a chunk have nearly the same
-// box and the same in-ellipse rows.  At set-up, union_batches_kernel groups each
+// Events are sorted by image tile, then by tan in buckets of 1/8, their box
+// corner inside the tile and tan (strip_sort.cu), so neighbouring events in a
+// chunk have nearly the same box and the same in-ellipse rows.  At set-up, union_batches_kernel groups each
 // chunk's events greedily into batches of up to E consecutive events whose
 // union -- per window row, from the smallest first column (rounded down to
 // even) to the largest last column -- spans at most 64 rows and 32 columns.  An
@@ -36,6 +36,18 @@
 // one FADD2 more per pair.  The coefficients p', q' are regenerated on chip for
 // every batch from the event's constants and the row (no per-row coefficient
 // table in memory).
+//
+// Chain form (the default where the row Gaussian spans several pixels,
+// |c| <= 0.06, e.g. 2 mm or 1 mm pixels at sigma_z = 5 pixels): along a row
+// K' = 2^(p' + q' jc) is geometric, so a lane evaluates two ex2 per event and
+// row (its first pixel pair) and steps to its next pair, 8 columns on, with one
+// FMUL2 by R8 = 2^(8 q') (computed once per event and row at set-up).  Every
+// K' a lane forms is a product of at most four rounded factors, within ~1e-6
+// of the direct value, and stays a normal float: a column of the union row is
+// at most ~43 pixels from the event's row peak, where 2^(c 43^2) >= 2^-111.
+// The masked K' stay in registers; the forward sum takes K' rho'' in one FFMA2
+// per pair, and the back-projection forms sum_e K'_e inv_e per pair and
+// multiplies by rho'' once per batch.
 //
 // Pixel set: exactly the reference's (gaussian_kernel.h:131-137 in its
 // rounding), from the exact per-row intervals of row_table_kernel: an event's
@@ -97,7 +109,7 @@ struct UStage {
 template <int E>
 struct USmem {
   UStage<E> stage[2];
-  float4 pq[2][E][kUPqStride];      // {p, p, q, q} per (event, union row)
+  float4 pq[2][E][kUPqStride];      // {p, p, q, q}, chain form {p, q, R8, R8}
   uint32_t mask[2][E][kUMaskStride];  // columns of the union row inside the event's interval
   uint32_t urow[2][kURows];     // union start column | union width << 16
   float den_part[2][E][kUMaxE];
@@ -128,7 +140,12 @@ __device__ __forceinline__ void u_issue_stage(UStage<E>& st, const UEvConst* __r
 
 // Union rows and per-(event, row) records of one batch: NW / 2 threads per
 // union row (consecutive lanes), each handling two events.
-template <int E, int NW>
+// Exponent forms of the iteration kernel (template argument XM).
+constexpr int kXFull = 0;   // p + q jc + c jc^2 per pixel
+constexpr int kXSplit = 1;  // 2^(c jc^2) folded into rho''
+constexpr int kXChain = 2;  // split, and K' stepped along the row by R8
+
+template <int E, int NW, int XM>
 __device__ __forceinline__ void u_setup(const DevGeom& g, const FastConst& fc, USmem<E>& S,
                                         int buf, uint32_t bw, int ox, int oy) {
   constexpr int kTPR = NW / 2;  // threads per union row
@@ -176,7 +193,12 @@ __device__ __forceinline__ void u_setup(const DevGeom& g, const FastConst& fc, U
     const int w = width[k];
     const int lr = first[k] - u;  // 0 <= lr, lr + w <= wu <= 32
     const uint32_t bits = (w >= 32) ? 0xFFFFFFFFu : ((1u << w) - 1u);
-    S.pq[buf][j][r] = make_float4(p, p, q, q);
+    if (XM == kXChain) {
+      const float r8 = ex2_approx(8.0f * q);
+      S.pq[buf][j][r] = make_float4(p, q, r8, r8);
+    } else {
+      S.pq[buf][j][r] = make_float4(p, p, q, q);
+    }
     S.mask[buf][j][r] = w > 0 ? (bits << lr) : 0u;
   }
 }
@@ -219,6 +241,62 @@ __device__ __forceinline__ void u_forward(float2 (&kr)[E][RS][kUSW], float (&dsu
   }
 }
 
+// Forward sums of one row step in the chain form: per event two ex2 for the
+// lane's first pixel pair, then one FMUL2 by R8 per further pair; the masked
+// K' stay in kr and the sum takes K' rho'' with one FFMA2 per pair.
+template <int E, int SWN, int RSI, int RS>
+__device__ __forceinline__ void u_forward_chain(float2 (&kr)[E][RS][kUSW], float (&dsum)[E],
+                                                const float* w_rho, const USmem<E>& S, int buf,
+                                                int base, int r_u, float jc0, int gl) {
+  float2 rr[kUSW];
+#pragma unroll
+  for (int s = 0; s < SWN; ++s) {
+    const float2 rv = *reinterpret_cast<const float2*>(w_rho + base + 8 * s);
+    const float2 gv = *reinterpret_cast<const float2*>(&S.gfac[2 * gl + 8 * s]);
+    rr[s] = __fmul2_rn(rv, gv);
+  }
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    const float4 a = S.pq[buf][j][r_u];
+    const uint32_t m = S.mask[buf][j][r_u] >> (2 * gl);
+    const float e0 = fmaf(a.y, jc0, a.x);
+    float2 k = make_float2(ex2_approx(e0), ex2_approx(e0 + a.y));
+    const float2 r8 = make_float2(a.z, a.w);
+    float2 dd;
+#pragma unroll
+    for (int s = 0; s < SWN; ++s) {
+      if (s > 0) k = __fmul2_rn(k, r8);
+      float2 v;
+      v.x = (m & (1u << (8 * s))) ? k.x : 0.0f;
+      v.y = (m & (2u << (8 * s))) ? k.y : 0.0f;
+      kr[j][RSI][s] = v;
+      dd = (s == 0) ? __fmul2_rn(v, rr[0]) : __ffma2_rn(v, rr[s], dd);
+    }
+    dsum[j] += dd.x + dd.y;
+  }
+}
+
+// Back-projection of one row step in the chain form: rho'' sum_e K'_e inv_e
+// per owned pixel pair (rho'' read again), one read-modify-write of the pair.
+template <int E, int SWN, int RSI, int RS>
+__device__ __forceinline__ void u_back_chain(const float2 (&kr)[E][RS][kUSW],
+                                             const float2 (&inv2)[E], const float* w_rho,
+                                             const float* gfac, float* w_out, int base, int wu,
+                                             int gl) {
+#pragma unroll
+  for (int s = 0; s < SWN; ++s) {
+    float2 acc = __fmul2_rn(kr[0][RSI][s], inv2[0]);
+#pragma unroll
+    for (int j = 1; j < E; ++j) acc = __ffma2_rn(kr[j][RSI][s], inv2[j], acc);
+    if (2 * gl + 8 * s < wu) {
+      const float2 rv = *reinterpret_cast<const float2*>(w_rho + base + 8 * s);
+      const float2 gv = *reinterpret_cast<const float2*>(gfac + 2 * gl + 8 * s);
+      float2* op = reinterpret_cast<float2*>(w_out + base + 8 * s);
+      *op = __ffma2_rn(acc, __fmul2_rn(rv, gv), *op);
+    }
+  }
+}
+
 // Back-projection of one row step: sum_e K_e rho inv_e per owned pixel pair,
 // one read-modify-write of the pair (inside the union row's width).
 template <int E, int SWN, int RSI, int RS>
@@ -236,29 +314,52 @@ __device__ __forceinline__ void u_back(const float2 (&kr)[E][RS][kUSW], const fl
   }
 }
 
-template <int E, int RSI, int RS, bool SPLIT>
+template <int E, int SWN, int RSI, int RS, int XM>
+__device__ __forceinline__ void u_forward_x(float2 (&kr)[E][RS][kUSW], float (&dsum)[E],
+                                            const float* w_rho, const USmem<E>& S, int buf,
+                                            int base, int r_u, const float2 (&jc2)[kUSW],
+                                            int gl) {
+  if (XM == kXChain)
+    u_forward_chain<E, SWN, RSI, RS>(kr, dsum, w_rho, S, buf, base, r_u, jc2[0].x, gl);
+  else
+    u_forward<E, SWN, RSI, RS, XM == kXSplit>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl);
+}
+
+template <int E, int RSI, int RS, int XM>
 __device__ __forceinline__ void u_forward_dispatch(int nsw, float2 (&kr)[E][RS][kUSW],
                                                    float (&dsum)[E], const float* w_rho,
                                                    const USmem<E>& S, int buf, int base, int r_u,
                                                    const float2 (&jc2)[kUSW], int gl) {
   switch (nsw) {
-    case 4: u_forward<E, 4, RSI, RS, SPLIT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
-    case 3: u_forward<E, 3, RSI, RS, SPLIT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
-    case 2: u_forward<E, 2, RSI, RS, SPLIT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
-    case 1: u_forward<E, 1, RSI, RS, SPLIT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 4: u_forward_x<E, 4, RSI, RS, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 3: u_forward_x<E, 3, RSI, RS, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 2: u_forward_x<E, 2, RSI, RS, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 1: u_forward_x<E, 1, RSI, RS, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
     default: break;
   }
 }
 
-template <int E, int RSI, int RS>
+template <int E, int SWN, int RSI, int RS, int XM>
+__device__ __forceinline__ void u_back_x(const float2 (&kr)[E][RS][kUSW],
+                                         const float2 (&inv2)[E], const float* w_rho,
+                                         const float* gfac, float* w_out, int base, int wu,
+                                         int gl) {
+  if (XM == kXChain)
+    u_back_chain<E, SWN, RSI, RS>(kr, inv2, w_rho, gfac, w_out, base, wu, gl);
+  else
+    u_back<E, SWN, RSI, RS>(kr, inv2, w_out, base, wu, gl);
+}
+
+template <int E, int RSI, int RS, int XM>
 __device__ __forceinline__ void u_back_dispatch(int nsw, const float2 (&kr)[E][RS][kUSW],
-                                                const float2 (&inv2)[E], float* w_out, int base,
+                                                const float2 (&inv2)[E], const float* w_rho,
+                                                const float* gfac, float* w_out, int base,
                                                 int wu, int gl) {
   switch (nsw) {
-    case 4: u_back<E, 4, RSI, RS>(kr, inv2, w_out, base, wu, gl); break;
-    case 3: u_back<E, 3, RSI, RS>(kr, inv2, w_out, base, wu, gl); break;
-    case 2: u_back<E, 2, RSI, RS>(kr, inv2, w_out, base, wu, gl); break;
-    case 1: u_back<E, 1, RSI, RS>(kr, inv2, w_out, base, wu, gl); break;
+    case 4: u_back_x<E, 4, RSI, RS, XM>(kr, inv2, w_rho, gfac, w_out, base, wu, gl); break;
+    case 3: u_back_x<E, 3, RSI, RS, XM>(kr, inv2, w_rho, gfac, w_out, base, wu, gl); break;
+    case 2: u_back_x<E, 2, RSI, RS, XM>(kr, inv2, w_rho, gfac, w_out, base, wu, gl); break;
+    case 1: u_back_x<E, 1, RSI, RS, XM>(kr, inv2, w_rho, gfac, w_out, base, wu, gl); break;
     default: break;
   }
 }
@@ -268,7 +369,7 @@ constexpr int u_min_blocks() {
   return NW == 8 ? 2 : 4;
 }
 
-template <int NW, bool SPLIT>
+template <int NW, int XM>
 __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_kernel(
     DevGeom g, FastConst fc, Tiling t, const Chunk* __restrict__ chunks,
     const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
@@ -323,7 +424,7 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
   unsigned long long contrib = 0;
   cp_async_wait_all();
   __syncthreads();
-  if (nb > 0) u_setup<E, NW>(g, fc, S, 0, bws[0], ox, oy);
+  if (nb > 0) u_setup<E, NW, XM>(g, fc, S, 0, bws[0], ox, oy);
   __syncthreads();
 
   for (int b = 0; b < nb; ++b) {
@@ -346,14 +447,14 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
       wu[rs] = static_cast<int>(ur >> 16);
       nsw[rs] = (__reduce_max_sync(kFull, static_cast<unsigned>(wu[rs])) + 7) >> 3;
     }
-    u_forward_dispatch<E, 0, RS, SPLIT>(nsw[0], kr, dsum, w_rho, S, buf, base[0], 8 * warp + gid,
-                                        jc2, gl);
+    u_forward_dispatch<E, 0, RS, XM>(nsw[0], kr, dsum, w_rho, S, buf, base[0], 8 * warp + gid,
+                                     jc2, gl);
     if (RS > 1)
-      u_forward_dispatch<E, (RS > 1 ? 1 : 0), RS, SPLIT>(nsw[RS - 1], kr, dsum, w_rho, S, buf,
-                                                         base[RS - 1],
-                                                         kRowsPerStep + 8 * warp + gid, jc2, gl);
+      u_forward_dispatch<E, (RS > 1 ? 1 : 0), RS, XM>(nsw[RS - 1], kr, dsum, w_rho, S, buf,
+                                                      base[RS - 1],
+                                                      kRowsPerStep + 8 * warp + gid, jc2, gl);
     // ---- set-up of the next batch (its staged data was published by the last barrier)
-    if (b + 1 < nb) u_setup<E, NW>(g, fc, S, buf ^ 1, bws[b + 1], ox, oy);
+    if (b + 1 < nb) u_setup<E, NW, XM>(g, fc, S, buf ^ 1, bws[b + 1], ox, oy);
     {
       const float tot = rows_transpose_sum<E>(dsum);
       if (rows_lane_writes<E>(lane)) S.den_part[buf][rows_lane_event<E>(lane)][warp] = tot;
@@ -368,7 +469,7 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
 #pragma unroll
       for (int w = 1; w < NW; ++w) den += S.den_part[buf][jl][w];
       const bool ok = den > 0.0f;  // inv_denominator = 0 otherwise (reconstruction.h:290)
-      inv_l = ok ? __frcp_rn(den) : 0.0f;
+      inv_l = ok ? rcp_approx(den) : 0.0f;
       const unsigned okm = __ballot_sync(kFull, ok && lane < cnt);
       if (threadIdx.x == 0) contrib += __popc(okm);
     }
@@ -379,10 +480,10 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
       inv2[j] = make_float2(v, v);
     }
     // ---- back-projection into the owned pixel pairs
-    u_back_dispatch<E, 0, RS>(nsw[0], kr, inv2, w_out, base[0], wu[0], gl);
+    u_back_dispatch<E, 0, RS, XM>(nsw[0], kr, inv2, w_rho, S.gfac, w_out, base[0], wu[0], gl);
     if (RS > 1)
-      u_back_dispatch<E, (RS > 1 ? 1 : 0), RS>(nsw[RS - 1], kr, inv2, w_out, base[RS - 1],
-                                               wu[RS - 1], gl);
+      u_back_dispatch<E, (RS > 1 ? 1 : 0), RS, XM>(nsw[RS - 1], kr, inv2, w_rho, S.gfac, w_out,
+                                                   base[RS - 1], wu[RS - 1], gl);
   }
 
   // ---- events outside the batch rectangle: reference-order warp rasteriser
@@ -546,23 +647,31 @@ bool union_split_exponent(const DevGeom& g, const FastConst& fc) {
   return -cz * 256.0f <= 80.0f;
 }
 
+// whether the chain form applies: split, and the row Gaussian wide enough that
+// every K' a lane steps through stays a normal float (see the file comment)
+bool union_chain_exponent(const DevGeom& g, const FastConst& fc) {
+  const float cz = fc.kz * g.pixel_width * g.pixel_width;
+  return union_split_exponent(g, fc) && -cz <= 0.06f;
+}
+
+namespace {
+template <int NW>
+cudaError_t union_set_smem(int bytes) {
+  cudaError_t e = cudaFuncSetAttribute(iterate_union_kernel<NW, kXFull>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(iterate_union_kernel<NW, kXSplit>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(iterate_union_kernel<NW, kXChain>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return e;
+}
+}  // namespace
+
 cudaError_t union_prepare_kernel(const Tiling& t) {
   const int bytes = static_cast<int>(union_smem_bytes(t));
-  cudaError_t e;
-  if (t.threads == 256) {
-    e = cudaFuncSetAttribute(iterate_union_kernel<8, true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(iterate_union_kernel<8, false>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  } else {
-    e = cudaFuncSetAttribute(iterate_union_kernel<4, true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(iterate_union_kernel<4, false>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  }
-  return e;
+  return t.threads == 256 ? union_set_smem<8>(bytes) : union_set_smem<4>(bytes);
 }
 
 cudaError_t launch_union_setup(const DevGeom& g, const FastConst& fc, const Tiling& t,
@@ -591,15 +700,21 @@ cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Ti
   if (t.chunk_events > kUMaxChunk || (t.row_stride & 7) != 0 ||
       (t.threads != 128 && t.threads != 256))
     return cudaErrorInvalidValue;
-  const bool split = union_split_exponent(g, fc);
+  const int xm = union_chain_exponent(g, fc) ? kXChain
+                 : union_split_exponent(g, fc) ? kXSplit
+                                               : kXFull;
   const auto* evc = static_cast<const UEvConst*>(ev_const);
   const size_t smem = union_smem_bytes(t);
   if (t.threads == 256) {
-    auto* k = split ? iterate_union_kernel<8, true> : iterate_union_kernel<8, false>;
+    auto* k = xm == kXChain   ? iterate_union_kernel<8, kXChain>
+              : xm == kXSplit ? iterate_union_kernel<8, kXSplit>
+                              : iterate_union_kernel<8, kXFull>;
     k<<<n_chunks, 256, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, rows, batches, rho,
                                   out, counters);
   } else {
-    auto* k = split ? iterate_union_kernel<4, true> : iterate_union_kernel<4, false>;
+    auto* k = xm == kXChain   ? iterate_union_kernel<4, kXChain>
+              : xm == kXSplit ? iterate_union_kernel<4, kXSplit>
+                              : iterate_union_kernel<4, kXFull>;
     k<<<n_chunks, 128, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, rows, batches, rho,
                                   out, counters);
   }
