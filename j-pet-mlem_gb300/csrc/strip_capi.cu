@@ -85,6 +85,8 @@ struct jpet_strip {
   DevBuf<unsigned char> sort_tmp; // set-up sort: radix-sort scratch
   DevBuf<uint32_t> batches;       // batch-union kernel: batch words per chunk
   DevBuf<unsigned char> ev_const; // batch-union kernel: per-event constants
+  DevBuf<uint16_t> union_rows;    // batch-union kernel: union row words per batch
+  DevBuf<uint16_t> event_rows;    // batch-union kernel: event row words per event
   FastConst fc{};
   bool use_fast = false;
   bool use_union = false;
@@ -395,9 +397,14 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
       JPET_CUDA(h, h->batches.alloc(static_cast<size_t>(acc)), "cudaMalloc(batches)");
       JPET_CUDA(h, h->ev_const.alloc(static_cast<size_t>(acc) * union_event_bytes()),
                 "cudaMalloc(event constants)");
+      JPET_CUDA(h, h->union_rows.alloc(static_cast<size_t>(acc) * union_row_words()),
+                "cudaMalloc(union rows)");
+      JPET_CUDA(h, h->event_rows.alloc(static_cast<size_t>(acc) * union_row_words()),
+                "cudaMalloc(event rows)");
       JPET_CUDA(h, launch_union_setup(h->g, h->fc, t, h->chunks.p, h->n_chunks, acc,
                                       h->sorted_geom.p, h->sorted_box.p, h->row_table.p,
-                                      h->ev_const.p, h->batches.p, s),
+                                      h->ev_const.p, h->batches.p, h->union_rows.p,
+                                      h->event_rows.p, s),
                 "batch formation launch");
       JPET_CUDA(h, union_prepare_kernel(t), "batch-union kernel attributes");
     } else if (h->opts.variant == JPET_VARIANT_FAST || h->opts.variant == JPET_VARIANT_ROWS) {
@@ -660,6 +667,8 @@ int jpet_strip_destroy(jpet_strip_t* h) {
   h->sort_tmp.release();
   h->batches.release();
   h->ev_const.release();
+  h->union_rows.release();
+  h->event_rows.release();
   h->box_pixels.release();
   h->nll_acc.release();
   h->nll_grad_tmp.release();
@@ -749,7 +758,8 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
       if (h->use_union) {
         JPET_CUDA(h, launch_iterate_union(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
                                           h->sorted_geom.p, h->sorted_box.p, h->ev_const.p,
-                                          h->row_table.p, h->batches.p, h->rho.p, h->out.p,
+                                          h->event_rows.p, h->union_rows.p, h->batches.p,
+                                          h->rho.p, h->out.p,
                                           h->counters.p, s),
                   "iteration kernel launch");
       } else if (h->opts.variant == JPET_VARIANT_WARP) {

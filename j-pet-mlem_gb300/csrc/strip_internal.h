@@ -170,15 +170,21 @@ size_t union_event_bytes();
 size_t union_smem_bytes(const Tiling& t);
 bool union_split_exponent(const DevGeom& g, const FastConst& fc);
 cudaError_t union_prepare_kernel(const Tiling& t);
+// union_row_words(): 16-bit words per event of the union-row and event-row
+// arrays (urows: per batch, indexed by the batch word's position; erows: per
+// event), written by launch_union_setup from the row table.
+size_t union_row_words();
 cudaError_t launch_union_setup(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                Chunk* chunks, int32_t n_chunks, int32_t n_events,
                                const float4* ev_geom, const short4* ev_box, const uint16_t* rows,
-                               void* ev_const, uint32_t* batches, cudaStream_t s);
+                               void* ev_const, uint32_t* batches, uint16_t* urows,
+                               uint16_t* erows, cudaStream_t s);
 cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                  const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                  const short4* ev_box, const void* ev_const,
-                                 const uint16_t* rows, const uint32_t* batches, const float* rho,
-                                 float* out, DevCounters* counters, cudaStream_t s);
+                                 const uint16_t* erows, const uint16_t* urows,
+                                 const uint32_t* batches, const float* rho, float* out,
+                                 DevCounters* counters, cudaStream_t s);
 cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint16_t* rows, const float* rho,

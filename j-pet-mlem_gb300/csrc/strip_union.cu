@@ -6,10 +6,12 @@
 // chunk have nearly the same box and the same in-ellipse rows.  At set-up, union_batches_kernel groups each
 // chunk's events greedily into batches of up to E consecutive events whose
 // union -- per window row, from the smallest first column (rounded down to
-// even) to the largest last column -- spans at most 64 rows and 32 columns.  An
-// event that does not fit that rectangle on its own is rasterised in the
-// reference's order instead (the exact path); union_events_kernel stores each
-// event's constants (y, tan, exponent coefficients, window-relative box).
+// even) to the largest last column -- spans at most 64 rows and 32 columns, and
+// writes, per batch, each union row's start column and width and, per event
+// and union row, its in-ellipse interval relative to that start.  An event
+// that does not fit that rectangle on its own is rasterised in the reference's
+// order instead (the exact path); union_events_kernel stores each event's
+// constants (y, tan, exponent coefficients, window-relative box).
 //
 // The iteration kernel runs one CTA of NW warps per chunk (E = NW events per
 // batch), with the rho and back-projection windows of the tile in shared
@@ -98,12 +100,21 @@ __host__ __device__ inline uint32_t ubatch_word(int first, int cnt, int rows, in
 }
 __device__ __forceinline__ int ub_first(uint32_t w) { return static_cast<int>(w & 1023u); }
 __device__ __forceinline__ int ub_cnt(uint32_t w) { return static_cast<int>((w >> 10) & 15u); }
+__device__ __forceinline__ int ub_rows(uint32_t w) { return static_cast<int>((w >> 14) & 127u); }
 __device__ __forceinline__ int ub_u0(uint32_t w) { return static_cast<int>((w >> 21) & 127u); }
+
+// Union row word (per batch and union row): start column in the window | width << 9.
+__host__ __device__ inline uint16_t urow_word(int u, int wu) {
+  return static_cast<uint16_t>(u | (wu << 9));
+}
+// Event row word (per event and union row of its batch): first in-ellipse
+// column relative to the union row's start | width << 8 (0: no pixel).
 
 template <int E>
 struct UStage {
   UEvConst ev[E];
-  uint16_t rows[E][kUTabStride];
+  uint16_t rows[E][kUTabStride];  // event row words of the batch's union rows
+  uint16_t urows[kURows];         // union row words
 };
 
 template <int E>
@@ -112,14 +123,16 @@ struct USmem {
   float4 pq[2][E][kUPqStride];      // {p, p, q, q}, chain form {p, q, R8, R8}
   uint32_t mask[2][E][kUMaskStride];  // columns of the union row inside the event's interval
   uint32_t urow[2][kURows];     // union start column | union width << 16
-  float den_part[2][E][kUMaxE];
+  __align__(16) float den_part[2][E][kUMaxE];
   float gfac[kUCols];           // 2^(c jc^2), jc = j - 16 (split exponent)
   float cjc[kUCols];            // c jc^2 (full exponent)
+  uint32_t bw[kUMaxChunk];      // the chunk's batch words and exact-path list
 };
 
 template <int E>
 __device__ __forceinline__ void u_issue_stage(UStage<E>& st, const UEvConst* __restrict__ evc,
-                                              const uint16_t* __restrict__ rows, int stride,
+                                              const uint16_t* __restrict__ erows,
+                                              const uint16_t* __restrict__ urows, int bi,
                                               int first, int cnt) {
   const int tid = threadIdx.x;
   if (tid < 2 * E) {
@@ -128,12 +141,15 @@ __device__ __forceinline__ void u_issue_stage(UStage<E>& st, const UEvConst* __r
     const int e = first + (v ? j : 0);
     cp_async16(reinterpret_cast<float4*>(&st.ev[j]) + h,
                reinterpret_cast<const float4*>(evc + e) + h, v);
+  } else if (tid >= 2 * E && tid < 2 * E + kURows / 8) {
+    const int q = tid - 2 * E;
+    cp_async16(&st.urows[8 * q], urows + static_cast<size_t>(bi) * kURows + 8 * q, true);
   } else if (tid >= 32 && tid < 32 + E * (kURows / 8)) {
     const int k = tid - 32;
     const int j = k >> 3, q = k & 7;
-    const bool v = j < cnt && 8 * q < stride;
-    const size_t src = static_cast<size_t>(first + (v ? j : 0)) * stride + (v ? 8 * q : 0);
-    cp_async16(&st.rows[j][8 * q], rows + src, v);
+    const bool v = j < cnt;
+    const size_t src = static_cast<size_t>(first + (v ? j : 0)) * kURows + 8 * q;
+    cp_async16(&st.rows[j][8 * q], erows + src, v);
   }
   cp_async_commit();
 }
@@ -151,32 +167,20 @@ __device__ __forceinline__ void u_setup(const DevGeom& g, const FastConst& fc, U
   constexpr int kTPR = NW / 2;  // threads per union row
   static_assert(E == 2 * kTPR, "two events per set-up thread");
   const UStage<E>& st = S.stage[buf];
-  const int cnt = ub_cnt(bw), u0 = ub_u0(bw);
+  const int u0 = ub_u0(bw);
   const int r = threadIdx.x / kTPR, sub = threadIdx.x % kTPR;
-  int first[2], width[2];
-  int lo = INT_MAX, hi = INT_MIN;
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    const int j = 2 * sub + k;
-    const uint32_t box = st.ev[j].box;
-    const int ri = u0 + r - static_cast<int>(box & 255u);
-    const bool v = j < cnt && static_cast<unsigned>(ri) < ((box >> 8) & 255u);
-    const uint32_t e = v ? st.rows[j][v ? ri : 0] : 0u;
-    width[k] = static_cast<int>(e >> 8);
-    first[k] = static_cast<int>(box >> 16) + static_cast<int>(e & 255u);
-    if (width[k] > 0) {
-      lo = min(lo, first[k]);
-      hi = max(hi, first[k] + width[k]);
-    }
+  if ((threadIdx.x >> 5) * (32 / kTPR) >= ub_rows(bw)) {
+    // every row of this warp lies past the union: empty rows, no records
+    if (sub == 0) S.urow[buf][r] = 0u;
+    S.mask[buf][2 * sub][r] = 0u;
+    S.mask[buf][2 * sub + 1][r] = 0u;
+    return;
   }
-#pragma unroll
-  for (int o = 1; o < kTPR; o <<= 1) {
-    lo = min(lo, __shfl_xor_sync(kFull, lo, o));
-    hi = max(hi, __shfl_xor_sync(kFull, hi, o));
-  }
-  const bool any = lo != INT_MAX;
-  const int u = any ? (lo & ~1) : 0;
-  const int wu = any ? hi - u : 0;
+  // union row (start column, width) and the events' intervals relative to it,
+  // as the batch former wrote them (rows past the union, and events past the
+  // batch's count, read as 0: no pixel)
+  const uint32_t ur = st.urows[r];
+  const int u = static_cast<int>(ur & 511u), wu = static_cast<int>(ur >> 9);
   if (sub == 0) S.urow[buf][r] = static_cast<uint32_t>(u) | (static_cast<uint32_t>(wu) << 16);
   const float py = g.tl_y_half_h - static_cast<float>(oy + u0 + r) * g.pixel_height;
   const float colm = static_cast<float>(ox + u + 16);
@@ -190,8 +194,9 @@ __device__ __forceinline__ void u_setup(const DevGeom& g, const FastConst& fc, U
     const float ua = fmaf(colm, g.pixel_width, e.ub - dy * e.tn);
     const float p = fmaf(fc.kz * ua, ua, fmaf(e.ky * dy, dy, lf));
     const float q = kz2pw * ua;
-    const int w = width[k];
-    const int lr = first[k] - u;  // 0 <= lr, lr + w <= wu <= 32
+    const uint32_t ew = st.rows[j][r];
+    const int w = static_cast<int>(ew >> 8);
+    const int lr = static_cast<int>(ew & 255u);  // 0 <= lr, lr + w <= wu <= 32
     const uint32_t bits = (w >= 32) ? 0xFFFFFFFFu : ((1u << w) - 1u);
     if (XM == kXChain) {
       const float r8 = ex2_approx(8.0f * q);
@@ -272,28 +277,37 @@ __device__ __forceinline__ void u_forward_chain(float2 (&kr)[E][RS][kUSW], float
       kr[j][RSI][s] = v;
       dd = (s == 0) ? __fmul2_rn(v, rr[0]) : __ffma2_rn(v, rr[s], dd);
     }
-    dsum[j] += dd.x + dd.y;
+    dsum[j] = (RSI == 0) ? dd.x + dd.y : dsum[j] + (dd.x + dd.y);
   }
 }
 
 // Back-projection of one row step in the chain form: rho'' sum_e K'_e inv_e
 // per owned pixel pair (rho'' read again), one read-modify-write of the pair.
 template <int E, int SWN, int RSI, int RS>
-__device__ __forceinline__ void u_back_chain(const float2 (&kr)[E][RS][kUSW],
-                                             const float2 (&inv2)[E], const float* w_rho,
-                                             const float* gfac, float* w_out, int base, int wu,
-                                             int gl) {
+__device__ __forceinline__ void u_back_chain(const float2 (&kr)[E][RS][kUSW], float inv_l,
+                                             const float* w_rho, const float* gfac,
+                                             float* w_out, int base, int wu, int gl) {
+  // events outer, so that one event's 1/den is live at a time (lane j holds
+  // event j's); the per-pair sums take the events in the same order as before
+  float2 acc[kUSW];
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    const float v = __shfl_sync(kFull, inv_l, j);
+    const float2 i2 = make_float2(v, v);
+#pragma unroll
+    for (int s = 0; s < SWN; ++s)
+      acc[s] = (j == 0) ? __fmul2_rn(kr[0][RSI][s], i2) : __ffma2_rn(kr[j][RSI][s], i2, acc[s]);
+  }
 #pragma unroll
   for (int s = 0; s < SWN; ++s) {
-    float2 acc = __fmul2_rn(kr[0][RSI][s], inv2[0]);
-#pragma unroll
-    for (int j = 1; j < E; ++j) acc = __ffma2_rn(kr[j][RSI][s], inv2[j], acc);
-    if (2 * gl + 8 * s < wu) {
-      const float2 rv = *reinterpret_cast<const float2*>(w_rho + base + 8 * s);
-      const float2 gv = *reinterpret_cast<const float2*>(gfac + 2 * gl + 8 * s);
-      float2* op = reinterpret_cast<float2*>(w_out + base + 8 * s);
-      *op = __ffma2_rn(acc, __fmul2_rn(rv, gv), *op);
-    }
+    // loads stay inside the windows (a row's last pair ends before the next
+    // row's pitch plus the 64-float padding); the store is predicated on the
+    // union row's width, the only pixels this row group owns
+    const float2 rv = *reinterpret_cast<const float2*>(w_rho + base + 8 * s);
+    const float2 gv = *reinterpret_cast<const float2*>(gfac + 2 * gl + 8 * s);
+    float2* op = reinterpret_cast<float2*>(w_out + base + 8 * s);
+    const float2 nv = __ffma2_rn(acc[s], __fmul2_rn(rv, gv), *op);
+    if (2 * gl + 8 * s < wu) *op = nv;
   }
 }
 
@@ -340,26 +354,33 @@ __device__ __forceinline__ void u_forward_dispatch(int nsw, float2 (&kr)[E][RS][
 }
 
 template <int E, int SWN, int RSI, int RS, int XM>
-__device__ __forceinline__ void u_back_x(const float2 (&kr)[E][RS][kUSW],
-                                         const float2 (&inv2)[E], const float* w_rho,
-                                         const float* gfac, float* w_out, int base, int wu,
-                                         int gl) {
-  if (XM == kXChain)
-    u_back_chain<E, SWN, RSI, RS>(kr, inv2, w_rho, gfac, w_out, base, wu, gl);
-  else
+__device__ __forceinline__ void u_back_x(const float2 (&kr)[E][RS][kUSW], float inv_l,
+                                         const float* w_rho, const float* gfac, float* w_out,
+                                         int base, int wu, int gl) {
+  if (XM == kXChain) {
+    u_back_chain<E, SWN, RSI, RS>(kr, inv_l, w_rho, gfac, w_out, base, wu, gl);
+  } else {
+    float2 inv2[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      const float v = __shfl_sync(kFull, inv_l, j);
+      inv2[j] = make_float2(v, v);
+    }
     u_back<E, SWN, RSI, RS>(kr, inv2, w_out, base, wu, gl);
+  }
 }
 
+// nsw is warp-uniform (a warp maximum), so the shuffles inside run converged
 template <int E, int RSI, int RS, int XM>
 __device__ __forceinline__ void u_back_dispatch(int nsw, const float2 (&kr)[E][RS][kUSW],
-                                                const float2 (&inv2)[E], const float* w_rho,
+                                                float inv_l, const float* w_rho,
                                                 const float* gfac, float* w_out, int base,
                                                 int wu, int gl) {
   switch (nsw) {
-    case 4: u_back_x<E, 4, RSI, RS, XM>(kr, inv2, w_rho, gfac, w_out, base, wu, gl); break;
-    case 3: u_back_x<E, 3, RSI, RS, XM>(kr, inv2, w_rho, gfac, w_out, base, wu, gl); break;
-    case 2: u_back_x<E, 2, RSI, RS, XM>(kr, inv2, w_rho, gfac, w_out, base, wu, gl); break;
-    case 1: u_back_x<E, 1, RSI, RS, XM>(kr, inv2, w_rho, gfac, w_out, base, wu, gl); break;
+    case 4: u_back_x<E, 4, RSI, RS, XM>(kr, inv_l, w_rho, gfac, w_out, base, wu, gl); break;
+    case 3: u_back_x<E, 3, RSI, RS, XM>(kr, inv_l, w_rho, gfac, w_out, base, wu, gl); break;
+    case 2: u_back_x<E, 2, RSI, RS, XM>(kr, inv_l, w_rho, gfac, w_out, base, wu, gl); break;
+    case 1: u_back_x<E, 1, RSI, RS, XM>(kr, inv_l, w_rho, gfac, w_out, base, wu, gl); break;
     default: break;
   }
 }
@@ -373,9 +394,9 @@ template <int NW, int XM>
 __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_kernel(
     DevGeom g, FastConst fc, Tiling t, const Chunk* __restrict__ chunks,
     const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
-    const UEvConst* __restrict__ evc, const uint16_t* __restrict__ rows,
-    const uint32_t* __restrict__ batches, const float* __restrict__ rho, float* __restrict__ out,
-    DevCounters* counters) {
+    const UEvConst* __restrict__ evc, const uint16_t* __restrict__ erows,
+    const uint16_t* __restrict__ urows, const uint32_t* __restrict__ batches,
+    const float* __restrict__ rho, float* __restrict__ out, DevCounters* counters) {
   constexpr int E = NW;                      // events per batch
   constexpr int kRowsPerStep = NW * 8;       // union rows per step of all warps
   constexpr int RS = kURows / kRowsPerStep;  // row steps
@@ -391,15 +412,15 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gid = lane >> 2, gl = lane & 3;
   const int nb = c.n_batches;
-  const int stride = t.row_stride;
   const uint32_t* bws = batches + c.start;
-  auto issue = [&](int b, int buf) {
-    const uint32_t w = bws[b];
-    u_issue_stage<E>(S.stage[buf], evc, rows, stride, c.start + ub_first(w), ub_cnt(w));
+  auto issue = [&](int b, int buf, uint32_t w) {
+    u_issue_stage<E>(S.stage[buf], evc, erows, urows, c.start + b, c.start + ub_first(w),
+                     ub_cnt(w));
   };
 
-  if (nb > 0) issue(0, 0);
-  if (nb > 1) issue(1, 1);
+  if (nb > 0) issue(0, 0, bws[0]);
+  if (nb > 1) issue(1, 1, bws[1]);
+  for (int i = threadIdx.x; i < c.count; i += NW * 32) S.bw[i] = bws[i];
   for (int r = warp; r < t.win_h; r += NW) {
     const int gy = oy + r;
     for (int col = lane; col < pitch; col += 32) {
@@ -424,14 +445,14 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
   unsigned long long contrib = 0;
   cp_async_wait_all();
   __syncthreads();
-  if (nb > 0) u_setup<E, NW, XM>(g, fc, S, 0, bws[0], ox, oy);
+  if (nb > 0) u_setup<E, NW, XM>(g, fc, S, 0, S.bw[0], ox, oy);
   __syncthreads();
 
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
-    const uint32_t bw = bws[b];
+    const uint32_t bw = S.bw[b];
     const int cnt = ub_cnt(bw), u0 = ub_u0(bw);
-    if (b + 2 < nb) issue(b + 2, buf);
+    if (b + 2 < nb) issue(b + 2, buf, S.bw[b + 2]);
     // ---- forward: this warp's union rows of every event of the batch
     float2 kr[E][RS][kUSW];
     float dsum[E];
@@ -454,7 +475,7 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
                                                       base[RS - 1],
                                                       kRowsPerStep + 8 * warp + gid, jc2, gl);
     // ---- set-up of the next batch (its staged data was published by the last barrier)
-    if (b + 1 < nb) u_setup<E, NW, XM>(g, fc, S, buf ^ 1, bws[b + 1], ox, oy);
+    if (b + 1 < nb) u_setup<E, NW, XM>(g, fc, S, buf ^ 1, S.bw[b + 1], ox, oy);
     {
       const float tot = rows_transpose_sum<E>(dsum);
       if (rows_lane_writes<E>(lane)) S.den_part[buf][rows_lane_event<E>(lane)][warp] = tot;
@@ -465,24 +486,22 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
     float inv_l;
     {
       const int jl = lane & (E - 1);
-      float den = S.den_part[buf][jl][0];
-#pragma unroll
-      for (int w = 1; w < NW; ++w) den += S.den_part[buf][jl][w];
+      const float4* dp = reinterpret_cast<const float4*>(S.den_part[buf][jl]);
+      const float4 d0 = dp[0];
+      float den = (d0.x + d0.y) + (d0.z + d0.w);
+      if (NW == 8) {
+        const float4 d1 = dp[1];
+        den += (d1.x + d1.y) + (d1.z + d1.w);
+      }
       const bool ok = den > 0.0f;  // inv_denominator = 0 otherwise (reconstruction.h:290)
       inv_l = ok ? rcp_approx(den) : 0.0f;
       const unsigned okm = __ballot_sync(kFull, ok && lane < cnt);
       if (threadIdx.x == 0) contrib += __popc(okm);
     }
-    float2 inv2[E];
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-      const float v = __shfl_sync(kFull, inv_l, j);
-      inv2[j] = make_float2(v, v);
-    }
     // ---- back-projection into the owned pixel pairs
-    u_back_dispatch<E, 0, RS, XM>(nsw[0], kr, inv2, w_rho, S.gfac, w_out, base[0], wu[0], gl);
+    u_back_dispatch<E, 0, RS, XM>(nsw[0], kr, inv_l, w_rho, S.gfac, w_out, base[0], wu[0], gl);
     if (RS > 1)
-      u_back_dispatch<E, (RS > 1 ? 1 : 0), RS, XM>(nsw[RS - 1], kr, inv2, w_rho, S.gfac, w_out,
+      u_back_dispatch<E, (RS > 1 ? 1 : 0), RS, XM>(nsw[RS - 1], kr, inv_l, w_rho, S.gfac, w_out,
                                                    base[RS - 1], wu[RS - 1], gl);
   }
 
@@ -491,7 +510,7 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
   unsigned long long dummy_calls = 0, exact_path = 0;
   const int nx = c.n_exact;
   for (int k = warp; k < nx; k += NW) {
-    const int ei = c.start + static_cast<int>(bws[c.count - 1 - k]);
+    const int ei = c.start + static_cast<int>(S.bw[c.count - 1 - k]);
     WindowAccess acc{w_rho, w_out, ox, oy, pitch};
     process_event<kCpuReference>(g, 32, ev_geom[ei], ev_box[ei], acc, nullptr, dummy_calls,
                                  contrib);
@@ -546,7 +565,9 @@ __global__ void __launch_bounds__(256) union_batches_kernel(Chunk* __restrict__ 
                                                             const short4* __restrict__ ev_box,
                                                             const uint16_t* __restrict__ rows,
                                                             int32_t stride,
-                                                            uint32_t* __restrict__ batches) {
+                                                            uint32_t* __restrict__ batches,
+                                                            uint16_t* __restrict__ urows,
+                                                            uint16_t* __restrict__ erows) {
   const int lane = threadIdx.x & 31;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -568,6 +589,28 @@ __global__ void __launch_bounds__(256) union_batches_kernel(Chunk* __restrict__ 
     auto emit = [&]() {
       if (cnt > 0) {
         if (lane == 0) batches[c.start + nb] = ubatch_word(bstart, cnt, u1 - u0, u0);
+        // union row words of the batch, and each event's intervals relative to
+        // its union rows (lane: window rows lane + 32 k; the arrays start zeroed)
+        uint16_t* ub = urows + static_cast<size_t>(c.start + nb) * kURows;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int wr = lane + 32 * k, r = wr - u0;
+          if (r >= 0 && r < kURows && ulo[k] != INT_MAX) {
+            const int u = ulo[k] & ~1;
+            ub[r] = urow_word(u, uhi[k] - u);
+            for (int i = bstart; i < bstart + cnt; ++i) {
+              const short4 b = ev_box[c.start + i];
+              const int ri = wr - (b.y - oy);
+              if (ri < 0 || ri >= b.w - b.y) continue;
+              const uint32_t e = rows[static_cast<size_t>(c.start + i) * stride + ri];
+              const int w = static_cast<int>(e >> 8);
+              if (w == 0) continue;
+              const int f = (b.x - ox) + static_cast<int>(e & 255u);
+              erows[static_cast<size_t>(c.start + i) * kURows + r] =
+                  static_cast<uint16_t>((f - u) | (w << 8));
+            }
+          }
+        }
         ++nb;
       }
       reset();
@@ -677,28 +720,35 @@ cudaError_t union_prepare_kernel(const Tiling& t) {
 cudaError_t launch_union_setup(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                Chunk* chunks, int32_t n_chunks, int32_t n_events,
                                const float4* ev_geom, const short4* ev_box, const uint16_t* rows,
-                               void* ev_const, uint32_t* batches, cudaStream_t s) {
+                               void* ev_const, uint32_t* batches, uint16_t* urows,
+                               uint16_t* erows, cudaStream_t s) {
   if (n_events <= 0) return cudaSuccess;
   if (t.threads != 128 && t.threads != 256) return cudaErrorInvalidValue;
   union_events_kernel<<<(n_events + 255) / 256, 256, 0, s>>>(
       g, fc, t, n_events, ev_geom, ev_box, static_cast<UEvConst*>(ev_const));
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || n_chunks <= 0) return e;
+  const size_t words = static_cast<size_t>(n_events) * kURows * sizeof(uint16_t);
+  e = cudaMemsetAsync(urows, 0, words, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(erows, 0, words, s);
+  if (e != cudaSuccess) return e;
   int blocks = (n_chunks + 7) / 8;
   if (blocks > 152 * 16) blocks = 152 * 16;
   union_batches_kernel<<<blocks, 256, 0, s>>>(chunks, n_chunks, t.threads / 32, ev_box, rows,
-                                              t.row_stride, batches);
+                                              t.row_stride, batches, urows, erows);
   return cudaGetLastError();
 }
+
+size_t union_row_words() { return kURows; }
 
 cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                  const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                  const short4* ev_box, const void* ev_const,
-                                 const uint16_t* rows, const uint32_t* batches, const float* rho,
-                                 float* out, DevCounters* counters, cudaStream_t s) {
+                                 const uint16_t* erows, const uint16_t* urows,
+                                 const uint32_t* batches, const float* rho, float* out,
+                                 DevCounters* counters, cudaStream_t s) {
   if (n_chunks <= 0) return cudaSuccess;
-  if (t.chunk_events > kUMaxChunk || (t.row_stride & 7) != 0 ||
-      (t.threads != 128 && t.threads != 256))
+  if (t.chunk_events > kUMaxChunk || (t.threads != 128 && t.threads != 256))
     return cudaErrorInvalidValue;
   const int xm = union_chain_exponent(g, fc) ? kXChain
                  : union_split_exponent(g, fc) ? kXSplit
@@ -709,14 +759,14 @@ cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Ti
     auto* k = xm == kXChain   ? iterate_union_kernel<8, kXChain>
               : xm == kXSplit ? iterate_union_kernel<8, kXSplit>
                               : iterate_union_kernel<8, kXFull>;
-    k<<<n_chunks, 256, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, rows, batches, rho,
-                                  out, counters);
+    k<<<n_chunks, 256, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, erows, urows, batches,
+                                  rho, out, counters);
   } else {
     auto* k = xm == kXChain   ? iterate_union_kernel<4, kXChain>
               : xm == kXSplit ? iterate_union_kernel<4, kXSplit>
                               : iterate_union_kernel<4, kXFull>;
-    k<<<n_chunks, 128, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, rows, batches, rho,
-                                  out, counters);
+    k<<<n_chunks, 128, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, erows, urows, batches,
+                                  rho, out, counters);
   }
   return cudaGetLastError();
 }
