@@ -100,7 +100,6 @@ __host__ __device__ inline uint32_t ubatch_word(int first, int cnt, int rows, in
 }
 __device__ __forceinline__ int ub_first(uint32_t w) { return static_cast<int>(w & 1023u); }
 __device__ __forceinline__ int ub_cnt(uint32_t w) { return static_cast<int>((w >> 10) & 15u); }
-__device__ __forceinline__ int ub_rows(uint32_t w) { return static_cast<int>((w >> 14) & 127u); }
 __device__ __forceinline__ int ub_u0(uint32_t w) { return static_cast<int>((w >> 21) & 127u); }
 
 // Union row word (per batch and union row): start column in the window | width << 9.
@@ -126,7 +125,7 @@ struct USmem {
   __align__(16) float den_part[2][E][kUMaxE];
   float gfac[kUCols];           // 2^(c jc^2), jc = j - 16 (split exponent)
   float cjc[kUCols];            // c jc^2 (full exponent)
-  uint32_t bw[kUMaxChunk];      // the chunk's batch words and exact-path list
+  uint32_t bw[kUMaxChunk + 4];  // the chunk's batch words and exact-path list (+ one read past the last batch)
 };
 
 template <int E>
@@ -169,13 +168,6 @@ __device__ __forceinline__ void u_setup(const DevGeom& g, const FastConst& fc, U
   const UStage<E>& st = S.stage[buf];
   const int u0 = ub_u0(bw);
   const int r = threadIdx.x / kTPR, sub = threadIdx.x % kTPR;
-  if ((threadIdx.x >> 5) * (32 / kTPR) >= ub_rows(bw)) {
-    // every row of this warp lies past the union: empty rows, no records
-    if (sub == 0) S.urow[buf][r] = 0u;
-    S.mask[buf][2 * sub][r] = 0u;
-    S.mask[buf][2 * sub + 1][r] = 0u;
-    return;
-  }
   // union row (start column, width) and the events' intervals relative to it,
   // as the batch former wrote them (rows past the union, and events past the
   // batch's count, read as 0: no pixel)
@@ -197,14 +189,15 @@ __device__ __forceinline__ void u_setup(const DevGeom& g, const FastConst& fc, U
     const uint32_t ew = st.rows[j][r];
     const int w = static_cast<int>(ew >> 8);
     const int lr = static_cast<int>(ew & 255u);  // 0 <= lr, lr + w <= wu <= 32
-    const uint32_t bits = (w >= 32) ? 0xFFFFFFFFu : ((1u << w) - 1u);
+    // w low bits set (0 <= w <= 32): the clamped funnel shift of ~0 by 32 - w
+    const uint32_t bits = __funnelshift_rc(0xFFFFFFFFu, 0u, static_cast<unsigned>(32 - w));
     if (XM == kXChain) {
       const float r8 = ex2_approx(8.0f * q);
       S.pq[buf][j][r] = make_float4(p, q, r8, r8);
     } else {
       S.pq[buf][j][r] = make_float4(p, p, q, q);
     }
-    S.mask[buf][j][r] = w > 0 ? (bits << lr) : 0u;
+    S.mask[buf][j][r] = bits << lr;
   }
 }
 
@@ -339,6 +332,49 @@ __device__ __forceinline__ void u_forward_x(float2 (&kr)[E][RS][kUSW], float (&d
     u_forward<E, SWN, RSI, RS, XM == kXSplit>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl);
 }
 
+// One row step (RS == 1): forward sums, their transposed warp sum and the
+// set-up of the next batch's records in one straight-line block per sweep
+// count, so that the scheduler interleaves the set-up's loads, ex2/lg2 and the
+// sum's shuffles with the evaluation.  The set-up runs even after a chunk's last
+// batch (it then fills the unused buffer from stale staged data).
+template <int E, int NW, int SWN, int XM>
+__device__ __forceinline__ float u_forward_setup_x(float2 (&kr)[E][1][kUSW], float (&dsum)[E],
+                                                   const float* w_rho, USmem<E>& S, int buf,
+                                                   int base, int r_u, const float2 (&jc2)[kUSW],
+                                                   int gl, const DevGeom& g,
+                                                   const FastConst& fc, uint32_t bw_next,
+                                                   int ox, int oy) {
+  if (SWN > 0) u_forward_x<E, (SWN > 0 ? SWN : 1), 0, 1, XM>(kr, dsum, w_rho, S, buf, base, r_u,
+                                                              jc2, gl);
+  const float tot = rows_transpose_sum<E>(dsum);
+  u_setup<E, NW, XM>(g, fc, S, buf ^ 1, bw_next, ox, oy);
+  return tot;
+}
+
+template <int E, int NW, int XM>
+__device__ __forceinline__ float u_forward_setup_dispatch(
+    int nsw, float2 (&kr)[E][1][kUSW], float (&dsum)[E], const float* w_rho, USmem<E>& S,
+    int buf, int base, int r_u, const float2 (&jc2)[kUSW], int gl, const DevGeom& g,
+    const FastConst& fc, uint32_t bw_next, int ox, int oy) {
+  switch (nsw) {
+    case 4:
+      return u_forward_setup_x<E, NW, 4, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
+                                             bw_next, ox, oy);
+    case 3:
+      return u_forward_setup_x<E, NW, 3, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
+                                             bw_next, ox, oy);
+    case 2:
+      return u_forward_setup_x<E, NW, 2, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
+                                             bw_next, ox, oy);
+    case 1:
+      return u_forward_setup_x<E, NW, 1, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
+                                             bw_next, ox, oy);
+    default:
+      return u_forward_setup_x<E, NW, 0, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
+                                             bw_next, ox, oy);
+  }
+}
+
 template <int E, int RSI, int RS, int XM>
 __device__ __forceinline__ void u_forward_dispatch(int nsw, float2 (&kr)[E][RS][kUSW],
                                                    float (&dsum)[E], const float* w_rho,
@@ -468,18 +504,23 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
       wu[rs] = static_cast<int>(ur >> 16);
       nsw[rs] = (__reduce_max_sync(kFull, static_cast<unsigned>(wu[rs])) + 7) >> 3;
     }
-    u_forward_dispatch<E, 0, RS, XM>(nsw[0], kr, dsum, w_rho, S, buf, base[0], 8 * warp + gid,
-                                     jc2, gl);
-    if (RS > 1)
+    // ---- forward, and the set-up of the next batch (its staged data was
+    // published by the last barrier)
+    float tot;
+    if constexpr (RS == 1) {
+      tot = u_forward_setup_dispatch<E, NW, XM>(nsw[0], kr, dsum, w_rho, S, buf, base[0],
+                                                8 * warp + gid, jc2, gl, g, fc, S.bw[b + 1],
+                                                ox, oy);
+    } else {
+      u_forward_dispatch<E, 0, RS, XM>(nsw[0], kr, dsum, w_rho, S, buf, base[0],
+                                       8 * warp + gid, jc2, gl);
       u_forward_dispatch<E, (RS > 1 ? 1 : 0), RS, XM>(nsw[RS - 1], kr, dsum, w_rho, S, buf,
                                                       base[RS - 1],
                                                       kRowsPerStep + 8 * warp + gid, jc2, gl);
-    // ---- set-up of the next batch (its staged data was published by the last barrier)
-    if (b + 1 < nb) u_setup<E, NW, XM>(g, fc, S, buf ^ 1, S.bw[b + 1], ox, oy);
-    {
-      const float tot = rows_transpose_sum<E>(dsum);
-      if (rows_lane_writes<E>(lane)) S.den_part[buf][rows_lane_event<E>(lane)][warp] = tot;
+      if (b + 1 < nb) u_setup<E, NW, XM>(g, fc, S, buf ^ 1, S.bw[b + 1], ox, oy);
+      tot = rows_transpose_sum<E>(dsum);
     }
+    if (rows_lane_writes<E>(lane)) S.den_part[buf][rows_lane_event<E>(lane)][warp] = tot;
     if (b + 2 < nb) cp_async_wait_all();
     __syncthreads();
     // ---- denominators: lane j (mod E) adds the warps' partials of event j
