@@ -200,14 +200,14 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
                    Tiling& t) {
   // window pixels per array (rho, out): 12288 (~100 KiB per CTA, 2 CTAs per SM)
   // for 256-thread CTAs; 6144 (~55 KiB, 4 CTAs per SM) for the row-owned
-  // kernel's 128-thread CTAs and for the batch-union kernel (~66 KiB with its
-  // batch records, 2 CTAs of 256 threads per SM)
+  // kernel's 128-thread CTAs and for the batch-union kernel (~74 KiB with its
+  // batch records, ~98 KiB with the compensation window, 2 CTAs of 256
+  // threads per SM)
   const bool fast = o.mode == JPET_MODE_CPU_REFERENCE &&
                     (o.variant == JPET_VARIANT_FAST || o.variant == JPET_VARIANT_ROWS);
-  const bool union_fp32 = fast && o.variant == JPET_VARIANT_FAST &&
-                          o.precision == JPET_PRECISION_FP32;
+  const bool union_k = fast && o.variant == JPET_VARIANT_FAST;
   const bool rows4 = fast && o.block_threads != 256;
-  const int budget_px = (rows4 || union_fp32) ? 6144 : 12288;
+  const int budget_px = (rows4 || union_k) ? 6144 : 12288;
   auto pct = [&](const std::vector<int32_t>& h, double keep) {
     int64_t tail = static_cast<int64_t>(std::floor((1.0 - keep) * n_nonempty));
     int64_t acc = 0;
@@ -246,7 +246,7 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
   t.chunk_events = 512;
   // the FP32 batch-union kernel (FAST variant) defaults to 256-thread CTAs
   // (8 events per batch); the row-owned kernel to 128
-  t.threads = o.block_threads > 0 ? o.block_threads : (union_fp32 ? 256 : (rows4 ? 128 : 256));
+  t.threads = o.block_threads > 0 ? o.block_threads : (union_k ? 256 : (rows4 ? 128 : 256));
   t.group = 32;
   // one spare entry per event for its widest row; a multiple of 8 entries so
   // that every event's table starts on a 16-byte boundary
@@ -383,8 +383,7 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
               "event sort");
   }
   h->use_fast = h->opts.mode == JPET_MODE_CPU_REFERENCE && h->opts.variant != JPET_VARIANT_EXACT;
-  h->use_union = h->use_fast && h->opts.variant == JPET_VARIANT_FAST &&
-                 h->opts.precision == JPET_PRECISION_FP32;
+  h->use_union = h->use_fast && h->opts.variant == JPET_VARIANT_FAST;
   h->table_kernel_calls = 0;
   if (h->use_fast && acc > 0) {
     JPET_CUDA(h, h->row_table.alloc(static_cast<size_t>(acc) * t.row_stride),
@@ -406,7 +405,8 @@ int prepare_events(jpet_strip* h, const float* d_zu, const float* d_zd, const fl
                                       h->ev_const.p, h->batches.p, h->union_rows.p,
                                       h->event_rows.p, s),
                 "batch formation launch");
-      JPET_CUDA(h, union_prepare_kernel(t), "batch-union kernel attributes");
+      JPET_CUDA(h, union_prepare_kernel(t, precision_code(h->opts.precision)),
+                "batch-union kernel attributes");
     } else if (h->opts.variant == JPET_VARIANT_FAST || h->opts.variant == JPET_VARIANT_ROWS) {
       JPET_CUDA(h, h->row_pq.alloc(static_cast<size_t>(acc) * t.row_stride),
                 "cudaMalloc(row coefficients)");
@@ -759,8 +759,8 @@ int jpet_strip_iterate(jpet_strip_t* h, int n) {
         JPET_CUDA(h, launch_iterate_union(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,
                                           h->sorted_geom.p, h->sorted_box.p, h->ev_const.p,
                                           h->event_rows.p, h->union_rows.p, h->batches.p,
-                                          h->rho.p, h->out.p,
-                                          h->counters.p, s),
+                                          h->rho.p, h->out.p, aux, h->counters.p, prec, seed,
+                                          s),
                   "iteration kernel launch");
       } else if (h->opts.variant == JPET_VARIANT_WARP) {
         JPET_CUDA(h, launch_iterate_fast(h->g, h->fc, h->tiling, h->chunks.p, h->n_chunks,

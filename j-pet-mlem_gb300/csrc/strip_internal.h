@@ -167,9 +167,9 @@ cudaError_t sort_events(const Tiling& t, int64_t n, const float4* ev_geom, const
 // to 4 (128-thread CTAs) or 8 (256-thread CTAs) similar events per chunk
 // (set-up), and the FP32 iteration over them.
 size_t union_event_bytes();
-size_t union_smem_bytes(const Tiling& t);
+size_t union_smem_bytes(const Tiling& t, int precision);
 bool union_split_exponent(const DevGeom& g, const FastConst& fc);
-cudaError_t union_prepare_kernel(const Tiling& t);
+cudaError_t union_prepare_kernel(const Tiling& t, int precision);
 // union_row_words(): 16-bit words per event of the union-row and event-row
 // arrays (urows: per batch, indexed by the batch word's position; erows: per
 // event), written by launch_union_setup from the row table.
@@ -184,7 +184,8 @@ cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Ti
                                  const short4* ev_box, const void* ev_const,
                                  const uint16_t* erows, const uint16_t* urows,
                                  const uint32_t* batches, const float* rho, float* out,
-                                 DevCounters* counters, cudaStream_t s);
+                                 AuxImage aux, DevCounters* counters, int precision,
+                                 uint32_t seed, cudaStream_t s);
 cudaError_t launch_iterate_fast(const DevGeom& g, const FastConst& fc, const Tiling& t,
                                 const Chunk* chunks, int32_t n_chunks, const float4* ev_geom,
                                 const short4* ev_box, const uint16_t* rows, const float* rho,

@@ -59,6 +59,7 @@
 
 #include <climits>
 #include <cstdint>
+#include <type_traits>
 
 #include "strip_async.cuh"
 #include "strip_device.cuh"
@@ -116,13 +117,13 @@ struct UStage {
   uint16_t urows[kURows];         // union row words
 };
 
-template <int E>
+template <int E, class DT>
 struct USmem {
   UStage<E> stage[2];
   float4 pq[2][E][kUPqStride];      // {p, p, q, q}, chain form {p, q, R8, R8}
   uint32_t mask[2][E][kUMaskStride];  // columns of the union row inside the event's interval
   uint32_t urow[2][kURows];     // union start column | union width << 16
-  __align__(16) float den_part[2][E][kUMaxE];
+  __align__(16) DT den_part[2][E][kUMaxE];  // float, or double (FP64 denominators)
   float gfac[kUCols];           // 2^(c jc^2), jc = j - 16 (split exponent)
   float cjc[kUCols];            // c jc^2 (full exponent)
   uint32_t bw[kUMaxChunk + 4];  // the chunk's batch words and exact-path list (+ one read past the last batch)
@@ -160,8 +161,8 @@ constexpr int kXFull = 0;   // p + q jc + c jc^2 per pixel
 constexpr int kXSplit = 1;  // 2^(c jc^2) folded into rho''
 constexpr int kXChain = 2;  // split, and K' stepped along the row by R8
 
-template <int E, int NW, int XM>
-__device__ __forceinline__ void u_setup(const DevGeom& g, const FastConst& fc, USmem<E>& S,
+template <int E, int NW, int XM, class DT>
+__device__ __forceinline__ void u_setup(const DevGeom& g, const FastConst& fc, USmem<E, DT>& S,
                                         int buf, uint32_t bw, int ox, int oy) {
   constexpr int kTPR = NW / 2;  // threads per union row
   static_assert(E == 2 * kTPR, "two events per set-up thread");
@@ -203,9 +204,10 @@ __device__ __forceinline__ void u_setup(const DevGeom& g, const FastConst& fc, U
 
 // Forward sums of one row step with SWN active sweeps: rho'' of the owned
 // pixel pairs, then every event's K rho'' (masked to its interval).
-template <int E, int SWN, int RSI, int RS, bool SPLIT>
-__device__ __forceinline__ void u_forward(float2 (&kr)[E][RS][kUSW], float (&dsum)[E],
-                                          const float* w_rho, const USmem<E>& S, int buf, int base,
+template <int E, int SWN, int RSI, int RS, bool SPLIT, class DT>
+__device__ __forceinline__ void u_forward(float2 (&kr)[E][RS][kUSW], DT (&dsum)[E],
+                                          const float* w_rho, const USmem<E, DT>& S, int buf,
+                                          int base,
                                           int r_u, const float2 (&jc2)[kUSW], int gl) {
   float2 rr[kUSW], cq[kUSW];
 #pragma unroll
@@ -235,16 +237,16 @@ __device__ __forceinline__ void u_forward(float2 (&kr)[E][RS][kUSW], float (&dsu
       kr[j][RSI][s] = v;
       dd = __fadd2_rn(dd, v);
     }
-    dsum[j] += dd.x + dd.y;
+    dsum[j] += static_cast<DT>(dd.x + dd.y);
   }
 }
 
 // Forward sums of one row step in the chain form: per event two ex2 for the
 // lane's first pixel pair, then one FMUL2 by R8 per further pair; the masked
 // K' stay in kr and the sum takes K' rho'' with one FFMA2 per pair.
-template <int E, int SWN, int RSI, int RS>
-__device__ __forceinline__ void u_forward_chain(float2 (&kr)[E][RS][kUSW], float (&dsum)[E],
-                                                const float* w_rho, const USmem<E>& S, int buf,
+template <int E, int SWN, int RSI, int RS, class DT>
+__device__ __forceinline__ void u_forward_chain(float2 (&kr)[E][RS][kUSW], DT (&dsum)[E],
+                                                const float* w_rho, const USmem<E, DT>& S, int buf,
                                                 int base, int r_u, float jc0, int gl) {
   float2 rr[kUSW];
 #pragma unroll
@@ -270,16 +272,60 @@ __device__ __forceinline__ void u_forward_chain(float2 (&kr)[E][RS][kUSW], float
       kr[j][RSI][s] = v;
       dd = (s == 0) ? __fmul2_rn(v, rr[0]) : __ffma2_rn(v, rr[s], dd);
     }
-    dsum[j] = (RSI == 0) ? dd.x + dd.y : dsum[j] + (dd.x + dd.y);
+    // a lane's partial over its <= 8 pixels of the row in FP32; FP64 (DEN64)
+    // from the sums across lanes and warps on
+    const DT pr = static_cast<DT>(dd.x + dd.y);
+    dsum[j] = (RSI == 0) ? pr : dsum[j] + pr;
+  }
+}
+
+// Adds a pixel pair's batch value v (sum over the batch's events of
+// K rho / den) into the back-projection window, storing only where the row
+// group owns the pair (own):
+//   kAccFloat        plain float addition;
+//   kAccCompensated  float addition whose exact rounding error (Knuth's TwoSum)
+//                    joins the compensation window;
+//   kAccFixed        v rounded once to 2^-22 of an event with the batch's
+//                    dither (floor(v 2^22 + U), U uniform in [0, 1): unbiased)
+//                    and added to the integer window (order-independent sums;
+//                    a window pixel of a chunk of <= 512 events stays < 2^31).
+template <int ACC>
+__device__ __forceinline__ void u_accumulate(float* w_out, float* w_comp, int idx, float2 v,
+                                             bool own, float dither) {
+  if (ACC == kAccFixed) {
+    uint2* op = reinterpret_cast<uint2*>(w_out + idx);
+    const uint2 o = *op;
+    const uint32_t q0 = __float2uint_rn(fmaf(v.x, kFixedScale, dither));
+    const uint32_t q1 = __float2uint_rn(fmaf(v.y, kFixedScale, dither));
+    if (own) *op = make_uint2(o.x + q0, o.y + q1);
+  } else {
+    float2* op = reinterpret_cast<float2*>(w_out + idx);
+    const float2 o = *op;
+    const float2 n = __fadd2_rn(o, v);
+    if (ACC == kAccCompensated) {
+      float2* cp = reinterpret_cast<float2*>(w_comp + idx);
+      const float2 bp = __fadd2_rn(n, make_float2(-o.x, -o.y));
+      const float2 nb = __fadd2_rn(n, make_float2(-bp.x, -bp.y));
+      const float2 err = __fadd2_rn(__fadd2_rn(o, make_float2(-nb.x, -nb.y)),
+                                    __fadd2_rn(v, make_float2(-bp.x, -bp.y)));
+      const float2 cn = __fadd2_rn(*cp, err);
+      if (own) {
+        *op = n;
+        *cp = cn;
+      }
+    } else if (own) {
+      *op = n;
+    }
   }
 }
 
 // Back-projection of one row step in the chain form: rho'' sum_e K'_e inv_e
 // per owned pixel pair (rho'' read again), one read-modify-write of the pair.
-template <int E, int SWN, int RSI, int RS>
+template <int E, int SWN, int RSI, int RS, int ACC>
 __device__ __forceinline__ void u_back_chain(const float2 (&kr)[E][RS][kUSW], float inv_l,
                                              const float* w_rho, const float* gfac,
-                                             float* w_out, int base, int wu, int gl) {
+                                             float* w_out, float* w_comp, int base, int wu,
+                                             int gl, float dither) {
   // events outer, so that one event's 1/den is live at a time (lane j holds
   // event j's); the per-pair sums take the events in the same order as before
   float2 acc[kUSW];
@@ -298,38 +344,49 @@ __device__ __forceinline__ void u_back_chain(const float2 (&kr)[E][RS][kUSW], fl
     // union row's width, the only pixels this row group owns
     const float2 rv = *reinterpret_cast<const float2*>(w_rho + base + 8 * s);
     const float2 gv = *reinterpret_cast<const float2*>(gfac + 2 * gl + 8 * s);
-    float2* op = reinterpret_cast<float2*>(w_out + base + 8 * s);
-    const float2 nv = __ffma2_rn(acc[s], __fmul2_rn(rv, gv), *op);
-    if (2 * gl + 8 * s < wu) *op = nv;
+    const bool own = 2 * gl + 8 * s < wu;
+    if (ACC == kAccFloat) {
+      float2* op = reinterpret_cast<float2*>(w_out + base + 8 * s);
+      const float2 nv = __ffma2_rn(acc[s], __fmul2_rn(rv, gv), *op);
+      if (own) *op = nv;
+    } else {
+      u_accumulate<ACC>(w_out, w_comp, base + 8 * s, __fmul2_rn(acc[s], __fmul2_rn(rv, gv)),
+                        own, dither);
+    }
   }
 }
 
 // Back-projection of one row step: sum_e K_e rho inv_e per owned pixel pair,
 // one read-modify-write of the pair (inside the union row's width).
-template <int E, int SWN, int RSI, int RS>
+template <int E, int SWN, int RSI, int RS, int ACC>
 __device__ __forceinline__ void u_back(const float2 (&kr)[E][RS][kUSW], const float2 (&inv2)[E],
-                                       float* w_out, int base, int wu, int gl) {
+                                       float* w_out, float* w_comp, int base, int wu, int gl,
+                                       float dither) {
 #pragma unroll
   for (int s = 0; s < SWN; ++s) {
     float2 acc = __fmul2_rn(kr[0][RSI][s], inv2[0]);
 #pragma unroll
     for (int j = 1; j < E; ++j) acc = __ffma2_rn(kr[j][RSI][s], inv2[j], acc);
-    if (2 * gl + 8 * s < wu) {
-      float2* op = reinterpret_cast<float2*>(w_out + base + 8 * s);
-      *op = __fadd2_rn(*op, acc);
+    if (ACC == kAccFloat) {
+      if (2 * gl + 8 * s < wu) {
+        float2* op = reinterpret_cast<float2*>(w_out + base + 8 * s);
+        *op = __fadd2_rn(*op, acc);
+      }
+    } else {
+      u_accumulate<ACC>(w_out, w_comp, base + 8 * s, acc, 2 * gl + 8 * s < wu, dither);
     }
   }
 }
 
-template <int E, int SWN, int RSI, int RS, int XM>
-__device__ __forceinline__ void u_forward_x(float2 (&kr)[E][RS][kUSW], float (&dsum)[E],
-                                            const float* w_rho, const USmem<E>& S, int buf,
+template <int E, int SWN, int RSI, int RS, int XM, class DT>
+__device__ __forceinline__ void u_forward_x(float2 (&kr)[E][RS][kUSW], DT (&dsum)[E],
+                                            const float* w_rho, const USmem<E, DT>& S, int buf,
                                             int base, int r_u, const float2 (&jc2)[kUSW],
                                             int gl) {
   if (XM == kXChain)
-    u_forward_chain<E, SWN, RSI, RS>(kr, dsum, w_rho, S, buf, base, r_u, jc2[0].x, gl);
+    u_forward_chain<E, SWN, RSI, RS, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2[0].x, gl);
   else
-    u_forward<E, SWN, RSI, RS, XM == kXSplit>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl);
+    u_forward<E, SWN, RSI, RS, XM == kXSplit, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl);
 }
 
 // One row step (RS == 1): forward sums, their transposed warp sum and the
@@ -337,64 +394,66 @@ __device__ __forceinline__ void u_forward_x(float2 (&kr)[E][RS][kUSW], float (&d
 // count, so that the scheduler interleaves the set-up's loads, ex2/lg2 and the
 // sum's shuffles with the evaluation.  The set-up runs even after a chunk's last
 // batch (it then fills the unused buffer from stale staged data).
-template <int E, int NW, int SWN, int XM>
-__device__ __forceinline__ float u_forward_setup_x(float2 (&kr)[E][1][kUSW], float (&dsum)[E],
-                                                   const float* w_rho, USmem<E>& S, int buf,
+template <int E, int NW, int SWN, int XM, class DT>
+__device__ __forceinline__ DT u_forward_setup_x(float2 (&kr)[E][1][kUSW], DT (&dsum)[E],
+                                                const float* w_rho, USmem<E, DT>& S, int buf,
                                                    int base, int r_u, const float2 (&jc2)[kUSW],
                                                    int gl, const DevGeom& g,
                                                    const FastConst& fc, uint32_t bw_next,
                                                    int ox, int oy) {
-  if (SWN > 0) u_forward_x<E, (SWN > 0 ? SWN : 1), 0, 1, XM>(kr, dsum, w_rho, S, buf, base, r_u,
-                                                              jc2, gl);
-  const float tot = rows_transpose_sum<E>(dsum);
-  u_setup<E, NW, XM>(g, fc, S, buf ^ 1, bw_next, ox, oy);
+  if (SWN > 0)
+    u_forward_x<E, (SWN > 0 ? SWN : 1), 0, 1, XM, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2,
+                                                      gl);
+  const DT tot = rows_transpose_sum<E>(dsum);
+  u_setup<E, NW, XM, DT>(g, fc, S, buf ^ 1, bw_next, ox, oy);
   return tot;
 }
 
-template <int E, int NW, int XM>
-__device__ __forceinline__ float u_forward_setup_dispatch(
-    int nsw, float2 (&kr)[E][1][kUSW], float (&dsum)[E], const float* w_rho, USmem<E>& S,
+template <int E, int NW, int XM, class DT>
+__device__ __forceinline__ DT u_forward_setup_dispatch(
+    int nsw, float2 (&kr)[E][1][kUSW], DT (&dsum)[E], const float* w_rho, USmem<E, DT>& S,
     int buf, int base, int r_u, const float2 (&jc2)[kUSW], int gl, const DevGeom& g,
     const FastConst& fc, uint32_t bw_next, int ox, int oy) {
   switch (nsw) {
     case 4:
-      return u_forward_setup_x<E, NW, 4, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
+      return u_forward_setup_x<E, NW, 4, XM, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
                                              bw_next, ox, oy);
     case 3:
-      return u_forward_setup_x<E, NW, 3, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
+      return u_forward_setup_x<E, NW, 3, XM, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
                                              bw_next, ox, oy);
     case 2:
-      return u_forward_setup_x<E, NW, 2, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
+      return u_forward_setup_x<E, NW, 2, XM, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
                                              bw_next, ox, oy);
     case 1:
-      return u_forward_setup_x<E, NW, 1, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
+      return u_forward_setup_x<E, NW, 1, XM, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
                                              bw_next, ox, oy);
     default:
-      return u_forward_setup_x<E, NW, 0, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
+      return u_forward_setup_x<E, NW, 0, XM, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl, g, fc,
                                              bw_next, ox, oy);
   }
 }
 
-template <int E, int RSI, int RS, int XM>
+template <int E, int RSI, int RS, int XM, class DT>
 __device__ __forceinline__ void u_forward_dispatch(int nsw, float2 (&kr)[E][RS][kUSW],
-                                                   float (&dsum)[E], const float* w_rho,
-                                                   const USmem<E>& S, int buf, int base, int r_u,
+                                                   DT (&dsum)[E], const float* w_rho,
+                                                   const USmem<E, DT>& S, int buf, int base, int r_u,
                                                    const float2 (&jc2)[kUSW], int gl) {
   switch (nsw) {
-    case 4: u_forward_x<E, 4, RSI, RS, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
-    case 3: u_forward_x<E, 3, RSI, RS, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
-    case 2: u_forward_x<E, 2, RSI, RS, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
-    case 1: u_forward_x<E, 1, RSI, RS, XM>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 4: u_forward_x<E, 4, RSI, RS, XM, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 3: u_forward_x<E, 3, RSI, RS, XM, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 2: u_forward_x<E, 2, RSI, RS, XM, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
+    case 1: u_forward_x<E, 1, RSI, RS, XM, DT>(kr, dsum, w_rho, S, buf, base, r_u, jc2, gl); break;
     default: break;
   }
 }
 
-template <int E, int SWN, int RSI, int RS, int XM>
+template <int E, int SWN, int RSI, int RS, int XM, int ACC>
 __device__ __forceinline__ void u_back_x(const float2 (&kr)[E][RS][kUSW], float inv_l,
                                          const float* w_rho, const float* gfac, float* w_out,
-                                         int base, int wu, int gl) {
+                                         float* w_comp, int base, int wu, int gl, float dither) {
   if (XM == kXChain) {
-    u_back_chain<E, SWN, RSI, RS>(kr, inv_l, w_rho, gfac, w_out, base, wu, gl);
+    u_back_chain<E, SWN, RSI, RS, ACC>(kr, inv_l, w_rho, gfac, w_out, w_comp, base, wu, gl,
+                                       dither);
   } else {
     float2 inv2[E];
 #pragma unroll
@@ -402,21 +461,33 @@ __device__ __forceinline__ void u_back_x(const float2 (&kr)[E][RS][kUSW], float 
       const float v = __shfl_sync(kFull, inv_l, j);
       inv2[j] = make_float2(v, v);
     }
-    u_back<E, SWN, RSI, RS>(kr, inv2, w_out, base, wu, gl);
+    u_back<E, SWN, RSI, RS, ACC>(kr, inv2, w_out, w_comp, base, wu, gl, dither);
   }
 }
 
 // nsw is warp-uniform (a warp maximum), so the shuffles inside run converged
-template <int E, int RSI, int RS, int XM>
+template <int E, int RSI, int RS, int XM, int ACC>
 __device__ __forceinline__ void u_back_dispatch(int nsw, const float2 (&kr)[E][RS][kUSW],
                                                 float inv_l, const float* w_rho,
-                                                const float* gfac, float* w_out, int base,
-                                                int wu, int gl) {
+                                                const float* gfac, float* w_out, float* w_comp,
+                                                int base, int wu, int gl, float dither) {
   switch (nsw) {
-    case 4: u_back_x<E, 4, RSI, RS, XM>(kr, inv_l, w_rho, gfac, w_out, base, wu, gl); break;
-    case 3: u_back_x<E, 3, RSI, RS, XM>(kr, inv_l, w_rho, gfac, w_out, base, wu, gl); break;
-    case 2: u_back_x<E, 2, RSI, RS, XM>(kr, inv_l, w_rho, gfac, w_out, base, wu, gl); break;
-    case 1: u_back_x<E, 1, RSI, RS, XM>(kr, inv_l, w_rho, gfac, w_out, base, wu, gl); break;
+    case 4:
+      u_back_x<E, 4, RSI, RS, XM, ACC>(kr, inv_l, w_rho, gfac, w_out, w_comp, base, wu, gl,
+                                       dither);
+      break;
+    case 3:
+      u_back_x<E, 3, RSI, RS, XM, ACC>(kr, inv_l, w_rho, gfac, w_out, w_comp, base, wu, gl,
+                                       dither);
+      break;
+    case 2:
+      u_back_x<E, 2, RSI, RS, XM, ACC>(kr, inv_l, w_rho, gfac, w_out, w_comp, base, wu, gl,
+                                       dither);
+      break;
+    case 1:
+      u_back_x<E, 1, RSI, RS, XM, ACC>(kr, inv_l, w_rho, gfac, w_out, w_comp, base, wu, gl,
+                                       dither);
+      break;
     default: break;
   }
 }
@@ -426,22 +497,39 @@ constexpr int u_min_blocks() {
   return NW == 8 ? 2 : 4;
 }
 
-template <int NW, int XM>
+// Shared memory of the kernel: the rho and back-projection windows (and the
+// compensation window of the compensated modes), then the batch records.
+template <int NW, int ACC, bool DEN64>
+size_t u_smem(const Tiling& t) {
+  using DT = typename std::conditional<DEN64, double, float>::type;
+  return (ACC == kAccCompensated ? 3ull : 2ull) * fast_window_floats(t) * sizeof(float) +
+         sizeof(USmem<NW, DT>);
+}
+
+// ACC: kAccFloat (the FP32 iteration), kAccCompensated (tile windows with
+// TwoSum compensation, flushed into the FP32 image and its FP32 compensation
+// image), kAccFixed (integer tile windows flushed into the 64-bit fixed-point
+// image); DEN64: per-event denominators reduced in FP64.
+template <int NW, int XM, int ACC, bool DEN64>
 __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_kernel(
     DevGeom g, FastConst fc, Tiling t, const Chunk* __restrict__ chunks,
     const float4* __restrict__ ev_geom, const short4* __restrict__ ev_box,
     const UEvConst* __restrict__ evc, const uint16_t* __restrict__ erows,
     const uint16_t* __restrict__ urows, const uint32_t* __restrict__ batches,
-    const float* __restrict__ rho, float* __restrict__ out, DevCounters* counters) {
+    const float* __restrict__ rho, float* __restrict__ out, AuxImage aux, uint32_t seed,
+    DevCounters* counters) {
+  using DT = typename std::conditional<DEN64, double, float>::type;
   constexpr int E = NW;                      // events per batch
   constexpr int kRowsPerStep = NW * 8;       // union rows per step of all warps
   constexpr int RS = kURows / kRowsPerStep;  // row steps
+  constexpr int kWindows = ACC == kAccCompensated ? 3 : 2;
   extern __shared__ __align__(16) float smem[];
   const int pitch = fast_pitch(t);
   const int wfl = fast_window_floats(t);
   float* w_rho = smem;
   float* w_out = smem + wfl;
-  USmem<E>& S = *reinterpret_cast<USmem<E>*>(smem + 2 * wfl);
+  float* w_comp = ACC == kAccCompensated ? smem + 2 * wfl : nullptr;
+  USmem<E, DT>& S = *reinterpret_cast<USmem<E, DT>*>(smem + kWindows * wfl);
 
   const Chunk c = chunks[blockIdx.x];
   const int ox = c.ox & ~1, oy = c.oy;
@@ -463,6 +551,7 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
       const int gx = ox + col;
       w_rho[r * pitch + col] = (gy < g.n_y && gx < g.n_z) ? rho[gy * g.n_z + gx] : 0.0f;
       w_out[r * pitch + col] = 0.0f;
+      if (ACC == kAccCompensated) w_comp[r * pitch + col] = 0.0f;
     }
   }
   for (int i = threadIdx.x; i < 64; i += NW * 32) w_rho[t.win_h * pitch + i] = 0.0f;
@@ -481,7 +570,7 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
   unsigned long long contrib = 0;
   cp_async_wait_all();
   __syncthreads();
-  if (nb > 0) u_setup<E, NW, XM>(g, fc, S, 0, S.bw[0], ox, oy);
+  if (nb > 0) u_setup<E, NW, XM, DT>(g, fc, S, 0, S.bw[0], ox, oy);
   __syncthreads();
 
   for (int b = 0; b < nb; ++b) {
@@ -491,9 +580,9 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
     if (b + 2 < nb) issue(b + 2, buf, S.bw[b + 2]);
     // ---- forward: this warp's union rows of every event of the batch
     float2 kr[E][RS][kUSW];
-    float dsum[E];
+    DT dsum[E];
 #pragma unroll
-    for (int j = 0; j < E; ++j) dsum[j] = 0.0f;
+    for (int j = 0; j < E; ++j) dsum[j] = DT(0);
     int base[RS], wu[RS], nsw[RS];
 #pragma unroll
     for (int rs = 0; rs < RS; ++rs) {
@@ -506,18 +595,18 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
     }
     // ---- forward, and the set-up of the next batch (its staged data was
     // published by the last barrier)
-    float tot;
+    DT tot;
     if constexpr (RS == 1) {
-      tot = u_forward_setup_dispatch<E, NW, XM>(nsw[0], kr, dsum, w_rho, S, buf, base[0],
+      tot = u_forward_setup_dispatch<E, NW, XM, DT>(nsw[0], kr, dsum, w_rho, S, buf, base[0],
                                                 8 * warp + gid, jc2, gl, g, fc, S.bw[b + 1],
                                                 ox, oy);
     } else {
-      u_forward_dispatch<E, 0, RS, XM>(nsw[0], kr, dsum, w_rho, S, buf, base[0],
-                                       8 * warp + gid, jc2, gl);
-      u_forward_dispatch<E, (RS > 1 ? 1 : 0), RS, XM>(nsw[RS - 1], kr, dsum, w_rho, S, buf,
+      u_forward_dispatch<E, 0, RS, XM, DT>(nsw[0], kr, dsum, w_rho, S, buf, base[0],
+                                           8 * warp + gid, jc2, gl);
+      u_forward_dispatch<E, (RS > 1 ? 1 : 0), RS, XM, DT>(nsw[RS - 1], kr, dsum, w_rho, S, buf,
                                                       base[RS - 1],
                                                       kRowsPerStep + 8 * warp + gid, jc2, gl);
-      if (b + 1 < nb) u_setup<E, NW, XM>(g, fc, S, buf ^ 1, S.bw[b + 1], ox, oy);
+      if (b + 1 < nb) u_setup<E, NW, XM, DT>(g, fc, S, buf ^ 1, S.bw[b + 1], ox, oy);
       tot = rows_transpose_sum<E>(dsum);
     }
     if (rows_lane_writes<E>(lane)) S.den_part[buf][rows_lane_event<E>(lane)][warp] = tot;
@@ -527,23 +616,38 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
     float inv_l;
     {
       const int jl = lane & (E - 1);
-      const float4* dp = reinterpret_cast<const float4*>(S.den_part[buf][jl]);
-      const float4 d0 = dp[0];
-      float den = (d0.x + d0.y) + (d0.z + d0.w);
-      if (NW == 8) {
-        const float4 d1 = dp[1];
-        den += (d1.x + d1.y) + (d1.z + d1.w);
+      DT den;
+      if constexpr (DEN64) {
+        den = S.den_part[buf][jl][0];
+#pragma unroll
+        for (int w = 1; w < NW; ++w) den += S.den_part[buf][jl][w];
+      } else {
+        const float4* dp = reinterpret_cast<const float4*>(S.den_part[buf][jl]);
+        const float4 d0 = dp[0];
+        den = (d0.x + d0.y) + (d0.z + d0.w);
+        if (NW == 8) {
+          const float4 d1 = dp[1];
+          den += (d1.x + d1.y) + (d1.z + d1.w);
+        }
       }
-      const bool ok = den > 0.0f;  // inv_denominator = 0 otherwise (reconstruction.h:290)
-      inv_l = ok ? rcp_approx(den) : 0.0f;
+      const bool ok = den > DT(0);  // inv_denominator = 0 otherwise (reconstruction.h:290)
+      inv_l = ok ? rcp_approx(static_cast<float>(den)) : 0.0f;
       const unsigned okm = __ballot_sync(kFull, ok && lane < cnt);
       if (threadIdx.x == 0) contrib += __popc(okm);
     }
-    // ---- back-projection into the owned pixel pairs
-    u_back_dispatch<E, 0, RS, XM>(nsw[0], kr, inv_l, w_rho, S.gfac, w_out, base[0], wu[0], gl);
+    // ---- back-projection into the owned pixel pairs (fixed-point mode: one
+    // dither per batch, from the batch's position and the iteration's seed)
+    float dither = 0.0f;
+    if (ACC == kAccFixed) {
+      const uint32_t key = hash32(static_cast<uint32_t>(c.start + b) ^ seed);
+      dither = static_cast<float>(key >> 8) * 5.9604644775390625e-08f - 0.5f;
+    }
+    u_back_dispatch<E, 0, RS, XM, ACC>(nsw[0], kr, inv_l, w_rho, S.gfac, w_out, w_comp, base[0],
+                                       wu[0], gl, dither);
     if (RS > 1)
-      u_back_dispatch<E, (RS > 1 ? 1 : 0), RS, XM>(nsw[RS - 1], kr, inv_l, w_rho, S.gfac, w_out,
-                                                   base[RS - 1], wu[RS - 1], gl);
+      u_back_dispatch<E, (RS > 1 ? 1 : 0), RS, XM, ACC>(nsw[RS - 1], kr, inv_l, w_rho, S.gfac,
+                                                        w_out, w_comp, base[RS - 1], wu[RS - 1],
+                                                        gl, dither);
   }
 
   // ---- events outside the batch rectangle: reference-order warp rasteriser
@@ -552,9 +656,18 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
   const int nx = c.n_exact;
   for (int k = warp; k < nx; k += NW) {
     const int ei = c.start + static_cast<int>(S.bw[c.count - 1 - k]);
-    WindowAccess acc{w_rho, w_out, ox, oy, pitch};
-    process_event<kCpuReference>(g, 32, ev_geom[ei], ev_box[ei], acc, nullptr, dummy_calls,
-                                 contrib);
+    if (ACC == kAccFloat) {
+      WindowAccess acc{w_rho, w_out, ox, oy, pitch};
+      process_event<kCpuReference>(g, 32, ev_geom[ei], ev_box[ei], acc, nullptr, dummy_calls,
+                                   contrib);
+    } else {
+      // the other modes' windows hold compensated or integer sums: these events
+      // add into the FP32 image directly (combined with the second image after
+      // the iteration)
+      GlobalAccess gacc{rho, out, g.n_z};
+      process_event<kCpuReference>(g, 32, ev_geom[ei], ev_box[ei], gacc, nullptr, dummy_calls,
+                                   contrib);
+    }
     if (lane == 0) ++exact_path;
   }
   if (lane == 0 && contrib) atomicAdd(&counters->n_contributing, contrib);
@@ -564,8 +677,18 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
     const int gy = oy + r;
     for (int col = lane; col < pitch; col += 32) {
       const int gx = ox + col;
-      const float v = w_out[r * pitch + col];
-      if (v != 0.0f && gy < g.n_y && gx < g.n_z) atomicAdd(&out[gy * g.n_z + gx], v);
+      if (ACC == kAccFloat) {
+        const float v = w_out[r * pitch + col];
+        if (v != 0.0f && gy < g.n_y && gx < g.n_z) atomicAdd(&out[gy * g.n_z + gx], v);
+      } else if (ACC == kAccCompensated) {
+        const float v = w_out[r * pitch + col], cv = w_comp[r * pitch + col];
+        if ((v != 0.0f || cv != 0.0f) && gy < g.n_y && gx < g.n_z)
+          flush_compensated(out, aux.lo, gy * g.n_z + gx, v, cv);
+      } else {
+        const uint32_t q = reinterpret_cast<const uint32_t*>(w_out)[r * pitch + col];
+        if (q != 0u && gy < g.n_y && gx < g.n_z)
+          atomicAdd(&aux.q[gy * g.n_z + gx], static_cast<unsigned long long>(q));
+      }
     }
   }
 }
@@ -712,17 +835,22 @@ __global__ void __launch_bounds__(256) union_batches_kernel(Chunk* __restrict__ 
   }
 }
 
-template <int NW>
-size_t u_smem(const Tiling& t) {
-  return 2ull * fast_window_floats(t) * sizeof(float) + sizeof(USmem<NW>);
-}
-
 }  // namespace
 
 size_t union_event_bytes() { return sizeof(UEvConst); }
 
-size_t union_smem_bytes(const Tiling& t) {
-  return t.threads == 256 ? u_smem<8>(t) : u_smem<4>(t);
+size_t union_smem_bytes(const Tiling& t, int precision) {
+  const bool w8 = t.threads == 256;
+  switch (precision) {
+    case kPrecisionCompensated:
+      return w8 ? u_smem<8, kAccCompensated, false>(t) : u_smem<4, kAccCompensated, false>(t);
+    case kPrecisionCompensatedDen64:
+      return w8 ? u_smem<8, kAccCompensated, true>(t) : u_smem<4, kAccCompensated, true>(t);
+    case kPrecisionFixed:
+      return w8 ? u_smem<8, kAccFixed, false>(t) : u_smem<4, kAccFixed, false>(t);
+    default:
+      return w8 ? u_smem<8, kAccFloat, false>(t) : u_smem<4, kAccFloat, false>(t);
+  }
 }
 
 // whether 2^(c jc^2), |jc| <= 16, may multiply rho (see the file comment)
@@ -739,23 +867,78 @@ bool union_chain_exponent(const DevGeom& g, const FastConst& fc) {
 }
 
 namespace {
-template <int NW>
+template <int NW, int ACC, bool DEN64>
 cudaError_t union_set_smem(int bytes) {
-  cudaError_t e = cudaFuncSetAttribute(iterate_union_kernel<NW, kXFull>,
+  cudaError_t e = cudaFuncSetAttribute(iterate_union_kernel<NW, kXFull, ACC, DEN64>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(iterate_union_kernel<NW, kXSplit>,
+    e = cudaFuncSetAttribute(iterate_union_kernel<NW, kXSplit, ACC, DEN64>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(iterate_union_kernel<NW, kXChain>,
+    e = cudaFuncSetAttribute(iterate_union_kernel<NW, kXChain, ACC, DEN64>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   return e;
 }
+template <int NW>
+cudaError_t union_set_smem_mode(int precision, int bytes) {
+  switch (precision) {
+    case kPrecisionCompensated: return union_set_smem<NW, kAccCompensated, false>(bytes);
+    case kPrecisionCompensatedDen64: return union_set_smem<NW, kAccCompensated, true>(bytes);
+    case kPrecisionFixed: return union_set_smem<NW, kAccFixed, false>(bytes);
+    default: return union_set_smem<NW, kAccFloat, false>(bytes);
+  }
+}
+
+template <int NW, int ACC, bool DEN64>
+void union_launch(int xm, int n_chunks, size_t smem, cudaStream_t s, const DevGeom& g,
+                  const FastConst& fc, const Tiling& t, const Chunk* chunks,
+                  const float4* ev_geom, const short4* ev_box, const UEvConst* evc,
+                  const uint16_t* erows, const uint16_t* urows, const uint32_t* batches,
+                  const float* rho, float* out, AuxImage aux, uint32_t seed,
+                  DevCounters* counters) {
+  auto* k = xm == kXChain   ? iterate_union_kernel<NW, kXChain, ACC, DEN64>
+            : xm == kXSplit ? iterate_union_kernel<NW, kXSplit, ACC, DEN64>
+                            : iterate_union_kernel<NW, kXFull, ACC, DEN64>;
+  k<<<n_chunks, NW * 32, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, erows, urows, batches,
+                                    rho, out, aux, seed, counters);
+}
+
+template <int NW>
+void union_launch_mode(int precision, int xm, int n_chunks, size_t smem, cudaStream_t s,
+                       const DevGeom& g, const FastConst& fc, const Tiling& t,
+                       const Chunk* chunks, const float4* ev_geom, const short4* ev_box,
+                       const UEvConst* evc, const uint16_t* erows, const uint16_t* urows,
+                       const uint32_t* batches, const float* rho, float* out, AuxImage aux,
+                       uint32_t seed, DevCounters* counters) {
+  switch (precision) {
+    case kPrecisionCompensated:
+      union_launch<NW, kAccCompensated, false>(xm, n_chunks, smem, s, g, fc, t, chunks, ev_geom,
+                                               ev_box, evc, erows, urows, batches, rho, out, aux,
+                                               seed, counters);
+      break;
+    case kPrecisionCompensatedDen64:
+      union_launch<NW, kAccCompensated, true>(xm, n_chunks, smem, s, g, fc, t, chunks, ev_geom,
+                                              ev_box, evc, erows, urows, batches, rho, out, aux,
+                                              seed, counters);
+      break;
+    case kPrecisionFixed:
+      union_launch<NW, kAccFixed, false>(xm, n_chunks, smem, s, g, fc, t, chunks, ev_geom,
+                                         ev_box, evc, erows, urows, batches, rho, out, aux,
+                                         seed, counters);
+      break;
+    default:
+      union_launch<NW, kAccFloat, false>(xm, n_chunks, smem, s, g, fc, t, chunks, ev_geom,
+                                         ev_box, evc, erows, urows, batches, rho, out, aux,
+                                         seed, counters);
+      break;
+  }
+}
 }  // namespace
 
-cudaError_t union_prepare_kernel(const Tiling& t) {
-  const int bytes = static_cast<int>(union_smem_bytes(t));
-  return t.threads == 256 ? union_set_smem<8>(bytes) : union_set_smem<4>(bytes);
+cudaError_t union_prepare_kernel(const Tiling& t, int precision) {
+  const int bytes = static_cast<int>(union_smem_bytes(t, precision));
+  return t.threads == 256 ? union_set_smem_mode<8>(precision, bytes)
+                          : union_set_smem_mode<4>(precision, bytes);
 }
 
 cudaError_t launch_union_setup(const DevGeom& g, const FastConst& fc, const Tiling& t,
@@ -787,7 +970,8 @@ cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Ti
                                  const short4* ev_box, const void* ev_const,
                                  const uint16_t* erows, const uint16_t* urows,
                                  const uint32_t* batches, const float* rho, float* out,
-                                 DevCounters* counters, cudaStream_t s) {
+                                 AuxImage aux, DevCounters* counters, int precision,
+                                 uint32_t seed, cudaStream_t s) {
   if (n_chunks <= 0) return cudaSuccess;
   if (t.chunk_events > kUMaxChunk || (t.threads != 128 && t.threads != 256))
     return cudaErrorInvalidValue;
@@ -795,20 +979,13 @@ cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Ti
                  : union_split_exponent(g, fc) ? kXSplit
                                                : kXFull;
   const auto* evc = static_cast<const UEvConst*>(ev_const);
-  const size_t smem = union_smem_bytes(t);
-  if (t.threads == 256) {
-    auto* k = xm == kXChain   ? iterate_union_kernel<8, kXChain>
-              : xm == kXSplit ? iterate_union_kernel<8, kXSplit>
-                              : iterate_union_kernel<8, kXFull>;
-    k<<<n_chunks, 256, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, erows, urows, batches,
-                                  rho, out, counters);
-  } else {
-    auto* k = xm == kXChain   ? iterate_union_kernel<4, kXChain>
-              : xm == kXSplit ? iterate_union_kernel<4, kXSplit>
-                              : iterate_union_kernel<4, kXFull>;
-    k<<<n_chunks, 128, smem, s>>>(g, fc, t, chunks, ev_geom, ev_box, evc, erows, urows, batches,
-                                  rho, out, counters);
-  }
+  const size_t smem = union_smem_bytes(t, precision);
+  if (t.threads == 256)
+    union_launch_mode<8>(precision, xm, n_chunks, smem, s, g, fc, t, chunks, ev_geom, ev_box, evc,
+                         erows, urows, batches, rho, out, aux, seed, counters);
+  else
+    union_launch_mode<4>(precision, xm, n_chunks, smem, s, g, fc, t, chunks, ev_geom, ev_box, evc,
+                         erows, urows, batches, rho, out, aux, seed, counters);
   return cudaGetLastError();
 }
 
