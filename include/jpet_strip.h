@@ -72,17 +72,18 @@ typedef struct jpet_strip_geom {
                                         into an FP32 compensation image added at the end */
 #define JPET_PRECISION_FP64_DEN 2    /* as COMPENSATED, plus per-event denominators reduced
                                         in FP64 (the only FP64 arithmetic of the modes) */
-#define JPET_PRECISION_FIXED 3       /* deterministic image: each contribution rounded once to
-                                        2^-22 of an event (unbiased per-event dither), summed
-                                        with integer shared atomics per tile and 64-bit integer
-                                        atomics over tiles, converted to FP32 once */
+#define JPET_PRECISION_FIXED 3       /* deterministic image: each pixel's contribution of a
+                                        batch of events (FAST) or of one event (ROWS) rounded
+                                        once to 2^-22 of an event (unbiased dither), summed as
+                                        integers per tile and with 64-bit integer atomics over
+                                        tiles, converted to FP32 once */
 
 /* iteration kernel */
-#define JPET_VARIANT_FAST 0  /* default.  FP32: batch-union kernel -- batches of <= 8 similar
-                                events share one lane-to-pixel map, rho is read and the
-                                back-projection written once per batch, exp2-form kernel with
-                                packed f32x2, per-row coefficients regenerated on chip; other
-                                precisions: the ROWS kernel */
+#define JPET_VARIANT_FAST 0  /* default, every precision: batch-union kernel -- batches of
+                                <= 8 similar events share one lane-to-pixel map, rho is read
+                                and the back-projection written once per batch, exp2-form
+                                kernel with packed f32x2, per-row coefficients regenerated
+                                on chip */
 #define JPET_VARIANT_EXACT 1 /* every pixel evaluated in the reference's operation order */
 #define JPET_VARIANT_WARP 2  /* one warp per event, shared-memory atomics */
 #define JPET_VARIANT_ROWS 3  /* row-owned kernel: image rows owned by warps, one event at a
@@ -106,7 +107,7 @@ typedef struct jpet_strip_opts {
   int32_t tile_w;       /* image tile width in pixels, 0 = chosen by the tuner */
   int32_t tile_h;       /* image tile height in pixels, 0 = chosen by the tuner */
   int32_t block_threads;/* threads per CTA of the iteration kernel, 0 = default (256 for
-                           the FP32 FAST kernel: 8 events per batch; 128 for the ROWS kernel;
+                           the FAST kernel: 8 events per batch; 128 for the ROWS kernel;
                            both take 128 or 256; 256 otherwise) */
   int32_t variant;      /* JPET_VARIANT_*; the GPU-reference mode always runs EXACT */
   int32_t raster_shape; /* JPET_RASTER_*; events outside the shape take the exact path */

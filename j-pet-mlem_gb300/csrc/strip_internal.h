@@ -165,7 +165,9 @@ cudaError_t sort_events(const Tiling& t, int64_t n, const float4* ev_geom, const
                         cudaStream_t s);
 // Batch-union kernel (strip_union.cu): per-event constants and batches of up
 // to 4 (128-thread CTAs) or 8 (256-thread CTAs) similar events per chunk
-// (set-up), and the FP32 iteration over them.
+// (set-up), and the iteration over them in every accumulation mode (precision:
+// a FastPrecision code; aux: the second image of the compensated and
+// fixed-point modes; seed: the fixed-point dither's per-iteration seed).
 size_t union_event_bytes();
 size_t union_smem_bytes(const Tiling& t, int precision);
 bool union_split_exponent(const DevGeom& g, const FastConst& fc);

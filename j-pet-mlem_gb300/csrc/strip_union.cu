@@ -1,10 +1,12 @@
 // Batch-union MLEM iteration kernel for the CPU-reference semantics (the
-// default FP32 kernel), and the set-up passes that feed it.
+// default kernel of every accumulation mode), and the set-up passes that feed
+// it.
 //
 // Events are sorted by image tile, then by tan in buckets of 1/8, their box
 // corner inside the tile and tan (strip_sort.cu), so neighbouring events in a
-// chunk have nearly the same box and the same in-ellipse rows.  At set-up, union_batches_kernel groups each
-// chunk's events greedily into batches of up to E consecutive events whose
+// chunk have nearly the same box and the same in-ellipse rows.  At set-up,
+// union_batches_kernel groups each chunk's events greedily into batches of up
+// to E consecutive events whose
 // union -- per window row, from the smallest first column (rounded down to
 // even) to the largest last column -- spans at most 64 rows and 32 columns, and
 // writes, per batch, each union row's start column and width and, per event
@@ -23,8 +25,17 @@
 // shared-memory read-modify-write per batch (not per event); no pixel has two
 // writers in a batch and no atomics are issued.  The per-(event, row)
 // exponent coefficients and column masks of batch b + 1 are computed by all
-// threads while batch b is in flight (double-buffered), so a batch costs one
-// CTA barrier (the one that publishes the denominators).
+// threads in the same straight-line block as batch b's forward sums
+// (double-buffered), so a batch costs one CTA barrier (the one that publishes
+// the denominators).
+//
+// Accumulation modes (template argument ACC, DEN64): FP32 windows flushed with
+// float atomics; compensated windows (each batch's addition followed by
+// Knuth's TwoSum into a compensation window, flushed into the FP32 image and
+// its FP32 compensation image); FP64 denominators on top of that (lane
+// partials over <= 8 pixels in FP32, the sums across lanes and warps in FP64);
+// fixed-point integer windows (a batch's value rounded once to 2^-22 of an
+// event with a per-batch dither, flushed into the 64-bit integer image).
 //
 // Kernel value (src/2d/strip/gaussian_kernel.h:51-79, rewritten as in
 // strip_fast.cu): along a row the exponent of K / K_ref is p + q j + c j^2 with

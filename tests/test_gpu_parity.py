@@ -314,6 +314,37 @@ def test_compensated_precision_modes(golden, precision):
         assert e_comp <= 1.05 * e_plain + 1e-9, (e_comp, e_plain)
 
 
+@pytest.mark.parametrize("threads", [128, 256])
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP32, capi.PRECISION_FIXED,
+                                       capi.PRECISION_COMPENSATED, capi.PRECISION_FP64_DEN])
+def test_batch_union_kernel_every_precision_mode(precision, threads):
+    """The default (FAST) kernel in every accumulation mode on 2 mm events, where
+    it takes the chain form of the exponent (two ex2 per event, row and lane,
+    the further pixel pairs stepped by a constant ratio): each image matches
+    the reference float path and the counters match exactly; the fixed-point
+    image is the same bit for bit on a second run."""
+    ell = phantom.random_ellipse_phantom(seed=9)
+    ev = phantom.generate_events(ell, 8000, 450.0, 1000.0, 10.0, 42.0, seed=9)
+    args = (450.0, 1000.0, 450, 500, 2.0, 10.0, 42.0)
+    cg, og = capi.Geometry(*args), O.Geometry(*args)
+    want, st = O.mlem_f(og, ev, 2, threads=8)
+    imgs = []
+    for _ in range(2 if precision == capi.PRECISION_FIXED else 1):
+        with capi.StripReconstruction(cg, precision=precision, block_threads=threads) as rec:
+            rec.set_events(ev)
+            rec.iterate(2)
+            imgs.append(rec.rho.copy())
+            cnt = rec.counters()
+    # fixed point: one rounding to 2^-22 of an event per batch and pixel
+    tol = 3e-5 if precision == capi.PRECISION_FIXED else TOL_ITER
+    assert rel_l2(imgs[0], want) < tol
+    assert cnt["n_kernel_calls"] == st["n_kernel_calls"]
+    assert cnt["n_contributing"] == st["n_contributing"]
+    assert cnt["n_exact_path"] == 0 and cnt["n_oversize"] == 0, cnt
+    if precision == capi.PRECISION_FIXED:
+        assert np.array_equal(imgs[0], imgs[1])
+
+
 def test_precision_mode_argument_checks():
     g = capi.Geometry(450, 1000, 90, 100, 10, 10, 42)
     with pytest.raises(capi.StripError) as e:
