@@ -40,7 +40,8 @@ class HybridGeometry:
     widths: np.ndarray         # float32[n_lors]
     pixels: np.ndarray         # PIXEL_DTYPE[n_infos]
     positions: np.ndarray      # float32[n_infos]
-    weights: np.ndarray        # float32[n_infos] (system-matrix weights; zeros = computed)
+    weights: np.ndarray        # float32[n_planes_half * n_infos] (system-matrix weights,
+                               # plane-major; zeros = computed)
     info_begin: np.ndarray     # uint64[n_lors]
     info_end: np.ndarray       # uint64[n_lors]
     n_columns: int
@@ -54,6 +55,7 @@ class HybridGeometry:
     sigma_dl: float
     length: float
     radius: float
+    n_planes_half: int = 1     # planes of weights (> 1: one system matrix per plane half)
 
     @property
     def n_lors(self) -> int:
@@ -265,8 +267,24 @@ def from_arrays(d, prefix: str = "") -> HybridGeometry:
     stores them (keys <prefix>segments, ..., <prefix>grid, <prefix>params)."""
     gi = d[prefix + "grid"]
     pa = d[prefix + "params"]
+    h = int(gi[7]) if gi.shape[0] > 7 else 1
     return HybridGeometry(int(gi[0]), d[prefix + "segments"], d[prefix + "widths"],
                           d[prefix + "pixels"], d[prefix + "positions"],
                           d[prefix + "weights_in"], d[prefix + "info_begin"],
                           d[prefix + "info_end"], int(gi[1]), int(gi[2]), int(gi[3]),
-                          *[float(v) for v in pa])
+                          *[float(v) for v in pa], n_planes_half=h)
+
+
+def multiplane_weights(g: HybridGeometry, n_planes_half: int, seed: int = 0) -> HybridGeometry:
+    """The geometry with n_planes_half planes of seeded system-matrix weights
+    (what 3d_hybrid_reconstruction loads from one --system matrix per plane
+    half, reconstruction_cmd.cpp:340-358): plane 0 the given weights, plane k
+    those weights times a seeded factor in [0.5, 1.5) per info."""
+    import dataclasses
+
+    rng = np.random.default_rng(seed)
+    w0 = np.asarray(g.weights, f32)[:g.n_pixel_infos]
+    planes = [w0] + [(w0 * rng.uniform(0.5, 1.5, w0.shape[0])).astype(f32)
+                     for _ in range(1, n_planes_half)]
+    return dataclasses.replace(g, weights=np.concatenate(planes).astype(f32),
+                               n_planes_half=n_planes_half)

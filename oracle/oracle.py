@@ -266,6 +266,8 @@ class OrcHybrid(C.Structure):
         ("sigma_z", C.c_float),
         ("sigma_dl", C.c_float),
         ("length", C.c_float),
+        ("n_planes_half", C.c_int32),
+        ("sens_depth", C.c_int32),
     ]
 
 
@@ -289,27 +291,47 @@ def _ptr(a) -> int:
     return a.ctypes.data if a.size else 0
 
 
-def hybrid_struct(g) -> tuple[OrcHybrid, list]:
+def hybrid_sens_depth(g, sens_given_3d: bool = False) -> int:
+    """Depth of the reconstruction's sensitivity image (reconstruction.h:80-85):
+    n_planes_half for a multi-plane geometry, n_planes / 2 with an external 3D
+    sensitivity, else 1."""
+    h = getattr(g, "n_planes_half", 1)
+    return h if h > 1 else (g.n_planes // 2 if sens_given_3d else 1)
+
+
+def hybrid_struct(g, sens_depth: int | None = None) -> tuple[OrcHybrid, list]:
     """orc_hybrid view of a HybridGeometry (arrays kept alive by the returned list)."""
     keep = [np.ascontiguousarray(a) for a in (g.segments, g.widths, g.pixels, g.positions,
                                                g.info_begin, g.info_end)]
+    h = getattr(g, "n_planes_half", 1)
+    d = hybrid_sens_depth(g) if sens_depth is None else sens_depth
     s = OrcHybrid(g.n_detectors, g.n_pixel_infos, *[_ptr(a) for a in keep], g.n_columns,
                   g.n_rows, g.n_planes, g.pixel_size, g.lower_left_x, g.lower_left_y, g.z_left,
-                  g.sigma_z, g.sigma_dl, g.length)
+                  g.sigma_z, g.sigma_dl, g.length, h, d)
     return s, keep
 
 
-def hybrid_setup(g, weights_given: bool = False, sens_to_one: bool = False):
-    """calculate_weight (unless given), calculate_sensitivity or ones, and
-    normalize_geometry_weights: (normalized weights, raw 2D sensitivity)."""
+def hybrid_setup(g, weights_given: bool = False, sens_to_one: bool = False,
+                 sens_given=None):
+    """calculate_weight (unless given), calculate_sensitivity, ones, or the given
+    3D sensitivity (float32[depth * n_rows * n_columns], the --sensitivity
+    image, depth n_planes / 2 or n_planes_half), then normalize_geometry_weights:
+    (normalized weights [n_planes_half * n_infos], raw sensitivity
+    [depth * n_rows * n_columns])."""
     L = _hyb_lib()
-    s, keep = hybrid_struct(g)
-    w = np.array(g.weights, np.float32, copy=True)
+    depth = hybrid_sens_depth(g, sens_given is not None)
+    s, keep = hybrid_struct(g, depth)
+    w = np.array(g.weights, np.float32, copy=True).reshape(-1)
     if not weights_given:
         L.orc_hybrid_calculate_weight(C.byref(s), _ptr(w))
-    sens = np.ones(g.n_columns * g.n_rows, np.float32)
-    if not sens_to_one:
-        L.orc_hybrid_calculate_sensitivity(C.byref(s), _ptr(w), _ptr(sens))
+    n_sens = depth * g.n_columns * g.n_rows
+    if sens_given is not None:
+        sens = np.array(sens_given, np.float32, copy=True).reshape(-1)
+        assert sens.size == n_sens
+    else:
+        sens = np.ones(n_sens, np.float32)
+        if not sens_to_one:
+            L.orc_hybrid_calculate_sensitivity(C.byref(s), _ptr(w), _ptr(sens))
     L.orc_hybrid_normalize(C.byref(s), _ptr(w), _ptr(sens))
     return w, sens
 
@@ -340,12 +362,12 @@ def hybrid_mlem(g, weights, sens, events, n_iterations: int, rho=None, threads: 
     counters int64[4]: used_events, used_pixels, used_voxels, positive denominators).
     release=True runs the timing build (FMA contraction allowed)."""
     L = _hyb_lib(release)
-    s, keep = hybrid_struct(g)
+    sn = np.ascontiguousarray(sens, np.float32).reshape(-1)
+    s, keep = hybrid_struct(g, sn.size // (g.n_columns * g.n_rows))
     rho = (np.ones(g.n_voxels, np.float32) if rho is None
            else np.array(rho, np.float32, copy=True).reshape(-1))
     ev = np.ascontiguousarray(events)
     w = np.ascontiguousarray(weights, np.float32)
-    sn = np.ascontiguousarray(sens, np.float32)
     cnt = np.zeros(4, np.int64)
     rc = L.orc_hybrid_mlem(C.byref(s), _ptr(w), _ptr(sn), _ptr(ev), ev.shape[0], _ptr(rho),
                            n_iterations, threads, _ptr(cnt))

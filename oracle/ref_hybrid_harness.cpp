@@ -1,12 +1,14 @@
 // Test-only harness: the reference's own 3D hybrid reconstruction,
 // PET3D::Hybrid::Reconstruction<Scanner, PET2D::Strip::GaussianKernel<float>>
 // (src/3d/hybrid/reconstruction.h), instantiated from the reference headers and
-// driven the way 3d_hybrid_reconstruction drives it without --sensitivity
-// (src/3d/hybrid/reconstruction_cmd.cpp:462-541): calculate_weight (unless the
-// weights are given, as with --system), calculate_sensitivity or
-// set_sensitivity_to_one (--sens-to-one), normalize_geometry_weights, the
-// responses read through operator<< (translate_to_frame and the bounding-box
-// filter), then operator() once per iteration.
+// driven the way 3d_hybrid_reconstruction drives it
+// (src/3d/hybrid/reconstruction_cmd.cpp:340-358, 462-541): calculate_weight
+// (unless the weights are given, as with --system, one matrix per plane half
+// for a multi-plane geometry), the external 3D sensitivity (--sensitivity),
+// set_sensitivity_to_one (--sens-to-one) or calculate_sensitivity,
+// normalize_geometry_weights, the responses read through operator<<
+// (translate_to_frame and the bounding-box filter), then operator() once per
+// iteration.
 //
 // The scanner is a harness class exposing the three things Reconstruction
 // reads from it (sigma_z(), sigma_dl(), length) and the Response type of
@@ -17,17 +19,19 @@
 //   case.txt (text):
 //     n_detectors n_pixel_infos n_columns n_rows n_planes
 //     pixel_size lower_left_x lower_left_y z_left sigma_z sigma_dl length
-//     weights_given sens_to_one n_iterations
+//     weights_given sens_to_one n_iterations [n_planes_half sens_given_3d]
 //     n_lors lines: 12 LineSegment fields (start, end, mid_point, direction,
 //                   normal, length, distance_from_origin), width, begin, end
-//     n_pixel_infos lines: x y position weight
+//     n_pixel_infos lines: x y position weight (n_planes_half weights: plane 0, 1, ...)
+//     with sens_given_3d: the sensitivity, (n_planes_half > 1 ? n_planes_half :
+//                   n_planes / 2) * n_rows * n_columns values, x fastest
 //     n_responses, then that many lines: first second z_up z_dn dl
 //   out.bin (little-endian):
 //     int64 n_events, then per event the FrameEvent fields
 //       int16 first, second; float up, right, tan, sec; uint64 begin, end;
 //       int16 plane_begin, plane_end
-//     float32 normalized weights [n_pixel_infos]
-//     float32 sensitivity [n_columns * n_rows]
+//     float32 normalized weights [n_planes_half * n_pixel_infos]
+//     float32 sensitivity [depth * n_columns * n_rows]
 //     per iteration: float32 rho [n_voxels], int64 used_events, used_pixels,
 //       used_voxels
 //
@@ -76,9 +80,17 @@ int main(int argc, char** argv) {
   if (!(in >> n_detectors >> n_infos >> n_columns >> n_rows >> n_planes)) return 3;
   if (!(in >> pixel_size >> llx >> lly >> z_left >> sigma_z >> sigma_dl >> length)) return 3;
   if (!(in >> weights_given >> sens_to_one >> n_iterations)) return 3;
+  int n_planes_half = 1, sens_given_3d = 0;
+  {
+    std::string rest;
+    std::getline(in, rest);
+    std::istringstream rs(rest);
+    if (rs >> n_planes_half) rs >> sens_given_3d;
+    if (n_planes_half < 1) n_planes_half = 1;
+  }
 
   using Geometry = Rec::Geometry;
-  Geometry geometry((short)n_detectors, (size_t)n_infos, 1);
+  Geometry geometry((short)n_detectors, (size_t)n_infos, (size_t)n_planes_half);
   for (size_t l = 0; l < geometry.n_lors; ++l) {
     float v[12], width;
     unsigned long long b, e;
@@ -99,23 +111,33 @@ int main(int argc, char** argv) {
   }
   for (long long i = 0; i < n_infos; ++i) {
     int x, y;
-    float pos, w;
-    if (!(in >> x >> y >> pos >> w)) return 3;
+    float pos;
+    if (!(in >> x >> y >> pos)) return 3;
     geometry.pixels[i] = PET2D::Pixel<short>((short)x, (short)y);
     geometry.pixel_positions[i] = pos;
-    geometry.pixel_weights[i] = w;
+    for (int plane = 0; plane < n_planes_half; ++plane) {
+      float w;
+      if (!(in >> w)) return 3;
+      geometry.pixel_weights[i + n_infos * plane] = w;
+    }
   }
 
   HarnessScanner scanner{sigma_z, sigma_dl, length};
   Rec::PixelGrid pixel_grid((short)n_columns, (short)n_rows, pixel_size,
                             PET2D::Point<float>(llx, lly));
   Rec::Grid grid(pixel_grid, z_left, (short)n_planes);
-  Rec rec(scanner, grid, geometry, false);
+  Rec rec(scanner, grid, geometry, sens_given_3d != 0);
   if (!weights_given) rec.calculate_weight();
-  if (sens_to_one)
+  const size_t n_sens = (size_t)rec.sensitivity.width * rec.sensitivity.height *
+                        rec.sensitivity.depth;
+  if (sens_given_3d) {
+    for (size_t i = 0; i < n_sens; ++i)
+      if (!(in >> rec.sensitivity.data[i])) return 3;
+  } else if (sens_to_one) {
     rec.set_sensitivity_to_one();
-  else
+  } else {
     rec.calculate_sensitivity();
+  }
   rec.normalize_geometry_weights();
 
   long long n_responses;
@@ -144,8 +166,8 @@ int main(int argc, char** argv) {
     put<int16_t>(out, e.plane_begin);
     put<int16_t>(out, e.plane_end);
   }
-  std::fwrite(geometry.pixel_weights, sizeof(float), (size_t)n_infos, out);
-  std::fwrite(rec.sensitivity.data, sizeof(float), (size_t)n_columns * n_rows, out);
+  std::fwrite(geometry.pixel_weights, sizeof(float), (size_t)n_infos * n_planes_half, out);
+  std::fwrite(rec.sensitivity.data, sizeof(float), n_sens, out);
   for (int it = 0; it < n_iterations; ++it) {
     rec();
     std::fwrite(rec.rho.data, sizeof(float), (size_t)grid.n_voxels, out);

@@ -168,6 +168,12 @@ typedef struct orc_hybrid {
   int32_t n_columns, n_rows, n_planes;
   float pixel_size, lower_left_x, lower_left_y, z_left;
   float sigma_z, sigma_dl, length;
+  /* GeometrySOA::n_planes_half (geometry_soa.h:283): planes of weights, each
+   * n_pixel_infos long (plane-major); > 1: the multi-plane system matrix */
+  int32_t n_planes_half;
+  /* depth of the sensitivity image (reconstruction.h:80-85): n_planes_half when
+   * > 1, else n_planes / 2 with an external 3D sensitivity, else 1 */
+  int32_t sens_depth;
 } orc_hybrid;
 
 void orc_hybrid_calculate_weight(const orc_hybrid* g, float* weights);

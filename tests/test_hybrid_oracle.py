@@ -2,7 +2,10 @@
 against the reference's own Reconstruction run on the same inputs
 (tests/golden/hybrid_ref.npz, made by make_hybrid_golden.py from the harness
 compiled out of src/3d/hybrid/reconstruction.h): weights, sensitivity, frame
-events and every iteration's image bit for bit, and the reference's statistics."""
+events and every iteration's image bit for bit, and the reference's statistics,
+in the single-plane form (computed or given weights), the multi-plane form (one
+system matrix per plane half, 3D sensitivity) and with an external 3D
+sensitivity."""
 import os
 
 import numpy as np
@@ -12,7 +15,13 @@ import oracle as O
 from jpet_strip import hybrid_workloads as H
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "hybrid_ref.npz")
-CASES = ("computed", "given")
+CASES = ("computed", "given", "multiplane", "sens3d")
+
+
+def setup(ref, tag, g):
+    gi = ref[tag + "_grid"]
+    sens_in = ref[tag + "_sens_in"] if tag + "_sens_in" in ref else None
+    return O.hybrid_setup(g, bool(gi[4]), bool(gi[5]), sens_given=sens_in)
 
 
 @pytest.fixture(scope="module")
@@ -23,8 +32,7 @@ def ref():
 @pytest.mark.parametrize("tag", CASES)
 def test_setup_and_frame_events_bit_exact(ref, tag):
     g = H.from_arrays(ref, tag + "_")
-    gi = ref[tag + "_grid"]
-    w, s = O.hybrid_setup(g, bool(gi[4]), bool(gi[5]))
+    w, s = setup(ref, tag, g)
     assert np.array_equal(w, ref[tag + "_weights"])
     assert np.array_equal(s, ref[tag + "_sens"])
     fr = O.hybrid_translate(g, w, ref[tag + "_responses"])
@@ -38,14 +46,17 @@ def test_setup_and_frame_events_bit_exact(ref, tag):
     lor = f * (f + 1) // 2 + fr["second"]
     assert np.any(fr["info_end"] == g.info_end[lor] + 1)
     assert np.any(fr["info_begin"] == g.info_begin[lor])
-    assert np.any(fr["plane_begin"] == 0) and np.any(fr["plane_end"] == g.n_planes)
+    # (the multi-plane and 3D-sensitivity cases start at plane 1: for plane 0 the
+    # reference reads one plane past its weight and sensitivity arrays)
+    first = 0 if g.n_planes_half == 1 and tag + "_sens_in" not in ref else 1
+    assert np.any(fr["plane_begin"] == first) and np.any(fr["plane_end"] == g.n_planes)
 
 
 @pytest.mark.parametrize("tag", CASES)
 def test_iterations_bit_exact(ref, tag):
     g = H.from_arrays(ref, tag + "_")
     gi = ref[tag + "_grid"]
-    w, s = O.hybrid_setup(g, bool(gi[4]), bool(gi[5]))
+    w, s = setup(ref, tag, g)
     fr = O.hybrid_translate(g, w, ref[tag + "_responses"])
     rho = None
     for it in range(int(gi[6])):
