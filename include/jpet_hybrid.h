@@ -9,8 +9,13 @@
  * calculate_sensitivity / set_sensitivity_to_one, normalize_geometry_weights and
  * translate_to_frame with the bounding-box filter (src/3d/hybrid/reconstruction.h:
  * 101-162, 218-274).  One iteration is Reconstruction::operator()
- * (reconstruction.h:276-446) with one plane half and the 2D sensitivity, the
- * configuration the command runs without --sensitivity and with one system matrix.
+ * (reconstruction.h:276-446) in each of its three forms: one plane half with the
+ * 2D sensitivity (one system matrix, no --sensitivity), one system matrix per
+ * plane half with the 3D sensitivity (n_planes_half > 1), and one plane half
+ * with an external 3D sensitivity (--sensitivity).  In the last two the voxels
+ * of plane iz read the weights and sensitivity of plane |iz - depth| (depth =
+ * n_planes_half or the sensitivity's depth); for plane 0 the reference's index
+ * is one plane past its arrays, and it is clamped to the last plane here.
  *
  * Plain C: pointers, sizes and the structs below, whose layouts are those of the
  * reference's own types with F = float, S = short and a 64-bit size_t, so that a
@@ -68,7 +73,7 @@ typedef struct jpet_hybrid_frame_event {
 } jpet_hybrid_frame_event;
 
 /* Host arrays of PET2D::Barrel::GeometrySOA<float, short>
- * (src/2d/barrel/geometry_soa.h:268-283, one plane half), the voxel grid
+ * (src/2d/barrel/geometry_soa.h:268-283), the voxel grid
  * (PET3D::VoxelGrid over PET2D::PixelGrid, src/3d/geometry/voxel_grid.h:22-26,
  * src/2d/geometry/pixel_grid.h:22-30) and the scanner values the reconstruction
  * reads (sigma_z(), sigma_dl(), length).  Lengths in the reference's unit. */
@@ -79,7 +84,8 @@ typedef struct jpet_hybrid_geom {
   const float* lor_widths;                 /* [n_lors] (used by computed weights) */
   const jpet_pixel* pixels;                /* [n_pixel_infos], each inside the grid */
   const float* pixel_positions;            /* [n_pixel_infos], ascending within a LOR */
-  const float* pixel_weights;              /* [n_pixel_infos] (given weights), or NULL */
+  const float* pixel_weights;              /* [n_planes_half * n_pixel_infos] (given weights,
+                                              plane-major as GeometrySOA stores them), or NULL */
   const uint64_t* lor_pixel_info_begin;    /* [n_lors] */
   const uint64_t* lor_pixel_info_end;      /* [n_lors] */
   int32_t n_columns, n_rows;               /* pixel grid */
@@ -89,6 +95,9 @@ typedef struct jpet_hybrid_geom {
   float z_left;                            /* VoxelGrid::z_left */
   float sigma_z, sigma_dl;                 /* TOF widths of the strip kernel */
   float length;                            /* scanner length */
+  int32_t n_planes_half;                   /* GeometrySOA::n_planes_half: 0 or 1 = one plane
+                                              half; > 1 = one system matrix per plane half
+                                              (the command loads n_planes / 2 of them) */
 } jpet_hybrid_geom;
 
 /* Where the pixel weights come from. */
@@ -101,13 +110,19 @@ typedef struct jpet_hybrid_geom {
 #define JPET_HYBRID_SENSITIVITY_COMPUTED 0 /* calculate_sensitivity (reconstruction.h:240-251),
                                               summed in pixel-info order */
 #define JPET_HYBRID_SENSITIVITY_ONE 1      /* set_sensitivity_to_one (--sens-to-one) */
-#define JPET_HYBRID_SENSITIVITY_GIVEN 2    /* opts->sensitivity, float[n_rows * n_columns] */
+#define JPET_HYBRID_SENSITIVITY_GIVEN 2    /* opts->sensitivity_map, float[n_rows * n_columns] */
+#define JPET_HYBRID_SENSITIVITY_GIVEN_3D 3 /* opts->sensitivity_map, the external 3D sensitivity
+                                              (--sensitivity): float[depth][n_rows][n_columns],
+                                              depth = n_planes_half if > 1, else n_planes / 2 */
+/* With n_planes_half > 1 the sensitivity is 3D (depth n_planes_half): COMPUTED sums
+ * each plane half's weights (reconstruction.h:240-251), ONE fills it, GIVEN_3D
+ * takes it; the weights must be given (GIVEN or NORMALIZED). */
 
 typedef struct jpet_hybrid_opts {
   int32_t device;              /* CUDA device ordinal */
   int32_t weights;             /* JPET_HYBRID_WEIGHTS_* */
   int32_t sensitivity;         /* JPET_HYBRID_SENSITIVITY_* */
-  const float* sensitivity_map;/* host float[n_rows * n_columns] for SENSITIVITY_GIVEN */
+  const float* sensitivity_map;/* host sensitivity for SENSITIVITY_GIVEN / GIVEN_3D */
   int32_t block_threads;       /* CTA size of the iteration kernel (0 = default, multiple of 32) */
   int32_t reserved;
 } jpet_hybrid_opts;
@@ -157,8 +172,9 @@ int jpet_hybrid_get_frame_events(jpet_hybrid_t* h, jpet_hybrid_frame_event* out,
  * (voxel_grid.h:54-56), host float[n_columns * n_rows * n_planes]. */
 int jpet_hybrid_set_image(jpet_hybrid_t* h, const float* rho);
 int jpet_hybrid_get_image(jpet_hybrid_t* h, float* rho);
-/* The 2D sensitivity (host float[n_columns * n_rows]) and the normalized pixel
- * weights (host float[n_pixel_infos]). */
+/* The sensitivity (host float[depth * n_columns * n_rows], depth 1 for the 2D
+ * sensitivity) and the normalized pixel weights (host
+ * float[n_planes_half * n_pixel_infos]). */
 int jpet_hybrid_get_sensitivity(jpet_hybrid_t* h, float* sens);
 int jpet_hybrid_get_weights(jpet_hybrid_t* h, float* weights);
 
@@ -169,7 +185,8 @@ int jpet_hybrid_get_counters(jpet_hybrid_t* h, jpet_hybrid_counters* out);
 int jpet_hybrid_synchronize(jpet_hybrid_t* h);
 
 /* The reference GPU entry point over host buffers (cuda/reconstruction.cu:36-187):
- * geometry with normalized weights, the sensitivity, frame events, and rho
+ * geometry with normalized weights, the sensitivity (2D, or 3D of depth
+ * n_planes_half for a multi-plane geometry), frame events, and rho
  * (in/out, reference voxel order); runs n_blocks * n_iterations_in_block
  * iterations, skipping those below start_iteration, and calls
  * output(iteration, image, user) where the reference does (after the first 5

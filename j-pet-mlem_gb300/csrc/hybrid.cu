@@ -74,7 +74,22 @@ struct HybConst {
   int32_t n_columns, n_rows, n_planes;
   int32_t n_lors;
   int64_t n_infos;
+  int32_t n_planes_half;  // planes of weights (> 1: one system matrix per plane half)
+  int32_t sens_depth;     // planes of the sensitivity image (1: the 2D sensitivity)
 };
+
+// Forms of the denominator loop (reconstruction.h:327-357):
+constexpr int kSens2D = 0;      // one plane half, 2D sensitivity
+constexpr int kMultiPlane = 1;  // weights and sensitivity of plane |iz - n_planes_half|
+constexpr int kSens3D = 2;      // one plane half, sensitivity of plane |iz - depth|
+
+// The plane of the weights / sensitivity that plane iz reads: |iz - depth|.
+// The reference's index reaches depth itself for plane 0 (and for the last
+// plane of an odd count), one plane past its arrays; clamped to depth - 1.
+__device__ __forceinline__ int abs_plane(int iz, int depth) {
+  const int a = iz > depth ? iz - depth : depth - iz;
+  return a < depth ? a : depth - 1;
+}
 
 // Sizes of the iteration kernel (compile-time; -D overrides for tuning sweeps).
 #ifndef JPET_HYBRID_THREADS
@@ -187,13 +202,16 @@ __global__ void unique_pixels_kernel(const int32_t* __restrict__ keys,
   }
 }
 
-// normalize_geometry_weights (reconstruction.h:253-272).
+// normalize_geometry_weights (reconstruction.h:253-272), every plane half:
+// weight (info, plane) / sensitivity (pixel, plane).
 __global__ void normalize_kernel(const int16_t* __restrict__ p16, int64_t n, HybConst c,
                                  const float* __restrict__ sens, float* __restrict__ w) {
+  const int64_t n_px = static_cast<int64_t>(c.n_columns) * c.n_rows;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const int x = p16[2 * i], y = p16[2 * i + 1];
-    w[i] = __fdiv_rn(w[i], sens[x + c.n_columns * y]);
+    for (int plane = 0; plane < c.n_planes_half; ++plane)
+      w[i + n * plane] = __fdiv_rn(w[i + n * plane], sens[x + c.n_columns * y + n_px * plane]);
   }
 }
 
@@ -383,6 +401,10 @@ __device__ __forceinline__ float rcp(float x) {
 
 // Per-pixel terms of GaussianKernel::operator() and ::sensitivity that do not
 // depend on z (gaussian_kernel.h:51-79,140-150) for pixel info i of the event.
+// Forms other than kSens2D keep in pa.w the info index (kMultiPlane: its weight
+// is the plane's) or the pixel weight times pi (kSens3D), and in pb.z the
+// pixel index (the sensitivity is the plane's).
+template <int SM>
 __device__ __forceinline__ void pixel_terms(const HybConst& c, const EvC& e, float4 s1,
                                             const int16_t* __restrict__ p16,
                                             const float* __restrict__ w,
@@ -409,9 +431,27 @@ __device__ __forceinline__ void pixel_terms(const HybConst& c, const EvC& e, flo
   const int pix = x + c.n_columns * y;
   // the exponent's z-independent part -log2(e) (r ipd r) / 2 and the pixel
   // weight times pi (the frame sensitivity's 1/pi) are folded in here
-  pa = make_float4(dy, ebe, brr * (-0.5f * 1.4426950408889634f), w[i] * kPi);
-  pb = make_float4(__frcp_rn(__fsub_rn(e.R, up)), __frcp_rn(__fadd_rn(e.R, up)), sens[pix],
+  const float wv = SM == kMultiPlane ? __int_as_float(static_cast<int>(i)) : w[i] * kPi;
+  const float sv = SM == kSens2D ? sens[pix] : __int_as_float(pix);
+  pa = make_float4(dy, ebe, brr * (-0.5f * 1.4426950408889634f), wv);
+  pb = make_float4(__frcp_rn(__fsub_rn(e.R, up)), __frcp_rn(__fadd_rn(e.R, up)), sv,
                    __int_as_float(pix * c.n_planes));
+}
+
+// The pixel weight (times pi) and the sensitivity a voxel of plane col uses.
+template <int SM>
+__device__ __forceinline__ float voxel_pixel_weight(const HybConst& c, const float4 pa, int col,
+                                                    const float* __restrict__ w) {
+  if (SM != kMultiPlane) return pa.w;
+  const int ap = abs_plane(col, c.n_planes_half);
+  return __ldg(&w[static_cast<int64_t>(ap) * c.n_infos + __float_as_int(pa.w)]) * kPi;
+}
+template <int SM>
+__device__ __forceinline__ float voxel_sens(const HybConst& c, const float4 pb, int col,
+                                            const float* __restrict__ sens) {
+  if (SM == kSens2D) return pb.z;
+  const int ap = abs_plane(col, SM == kMultiPlane ? c.n_planes_half : c.sens_depth);
+  return __ldg(&sens[static_cast<int64_t>(ap) * c.n_columns * c.n_rows + __float_as_int(pb.z)]);
 }
 
 // Arctangent of y / x in (-pi, pi]: reduction to r = min(|x|, |y|) / max(|x|, |y|)
@@ -444,24 +484,30 @@ __device__ __forceinline__ float atan2_poly(float y, float x) {
 // atan(a) - atan(b) (gaussian_kernel.h:140-150) is evaluated as
 // atan2(a - b, 1 + a b), the same angle for every a, b; a non-positive kernel
 // value gives weight 0 as in the reference (reconstruction.h:335-341).
+template <int SM>
 __device__ __forceinline__ float plane_weight(const HybConst& c, const EvC& e, const float4 pa,
                                               const float4 pb, float dz, float lp, float lm,
-                                              int col, const float* __restrict__ rho) {
+                                              int col, const float* __restrict__ rho,
+                                              const float* __restrict__ w) {
   const float bpq = fmaf(-pa.x, e.tan, dz);
   const float K = pa.y * ex2(fmaf(bpq * bpq, c.exp_bpq, pa.z));
   const float a = fminf(lm * pb.x, lp * pb.y);
   const float bb = fmaxf(-lp * pb.x, -lm * pb.y);
   const float ang = atan2_poly(a - bb, fmaf(a, bb, 1.0f));
-  const float v = (K * pa.w) * rcp(ang) * __ldg(&rho[__float_as_int(pb.w) + col]);
+  const float v = (K * voxel_pixel_weight<SM>(c, pa, col, w)) * rcp(ang) *
+                  __ldg(&rho[__float_as_int(pb.w) + col]);
   return ang < 0.0f ? 0.0f : v;
 }
 
 // The same for the event's k-th plane, z = z0 + k pixel_size.
+template <int SM>
 __device__ __forceinline__ float voxel_weight(const HybConst& c, const EvC& e, const float4 pa,
                                               const float4 pb, int k,
-                                              const float* __restrict__ rho) {
+                                              const float* __restrict__ rho,
+                                              const float* __restrict__ w) {
   const float z = fmaf(static_cast<float>(k), c.ps, e.z0);
-  return plane_weight(c, e, pa, pb, z - e.right, c.L2 + z, c.L2 - z, e.plane_begin + k, rho);
+  return plane_weight<SM>(c, e, pa, pb, z - e.right, c.L2 + z, c.L2 - z, e.plane_begin + k,
+                          rho, w);
 }
 
 // Advances a thread's (pixel, plane) position by one CTA-wide step of the
@@ -493,6 +539,7 @@ __device__ __forceinline__ float multiplicity(int64_t i, int dup, int64_t last) 
 // per event; each thread keeps its first kSteps weights in shared memory for
 // the back-projection.  Events with more than kPix infos or kThreads planes are
 // walked flattened, chunk by chunk, and recomputed in the back-projection.
+template <int SM>
 __global__ void __launch_bounds__(kThreads)
     iterate_kernel(const jpet_hybrid_frame_event* __restrict__ ev, int64_t n,
                    const float4* __restrict__ seg, const int16_t* __restrict__ p16,
@@ -543,7 +590,7 @@ __global__ void __launch_bounds__(kThreads)
       __syncthreads();
       for (int j = tid; j < ni; j += kThreads) {
         const int64_t info = static_cast<int64_t>(fe.pixel_info_begin) + j;
-        pixel_terms(c, e, s1, p16, w, sens, info, pa[j], pb[j]);
+        pixel_terms<SM>(c, e, s1, p16, w, sens, info, pa[j], pb[j]);
         if (j < ni - 1 && p32[info] == last_pixel) dup = j;
       }
       __syncthreads();
@@ -556,13 +603,14 @@ __global__ void __launch_bounds__(kThreads)
       float* cp = cache + tid;
       for (int t = 0; t < ncached; ++t, a += G, b += G, cp += kThreads) {
         const float4 bv = *b;
-        const float v = plane_weight(c, e, *a, bv, dz, lp, lm, col, rho);
-        den = fmaf(v, bv.z, den);
+        const float v = plane_weight<SM>(c, e, *a, bv, dz, lp, lm, col, rho, w);
+        den = fmaf(v, voxel_sens<SM>(c, bv, col, sens), den);
         *cp = v;
       }
       for (int t = ncached; t < nmine; ++t, a += G, b += G) {
         const float4 bv = *b;
-        den = fmaf(plane_weight(c, e, *a, bv, dz, lp, lm, col, rho), bv.z, den);
+        den = fmaf(plane_weight<SM>(c, e, *a, bv, dz, lp, lm, col, rho, w),
+                   voxel_sens<SM>(c, bv, col, sens), den);
       }
     } else {
       for (int64_t cb = 0; cb < nin; cb += kPix) {
@@ -570,12 +618,13 @@ __global__ void __launch_bounds__(kThreads)
         __syncthreads();
         for (int j = tid; j < cn; j += kThreads) {
           const int64_t info = static_cast<int64_t>(fe.pixel_info_begin) + cb + j;
-          pixel_terms(c, e, s1, p16, w, sens, info, pa[j], pb[j]);
+          pixel_terms<SM>(c, e, s1, p16, w, sens, info, pa[j], pb[j]);
           if (cb + j < nin - 1 && p32[info] == last_pixel) dup = static_cast<int>(cb + j);
         }
         __syncthreads();
         for (int i = i0, k = k0; i < cn; walk(i, k, q, r, npl))
-          den = fmaf(voxel_weight(c, e, pa[i], pb[i], k, rho), pb[i].z, den);
+          den = fmaf(voxel_weight<SM>(c, e, pa[i], pb[i], k, rho, w),
+                     voxel_sens<SM>(c, pb[i], e.plane_begin + k, sens), den);
       }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -613,13 +662,14 @@ __global__ void __launch_bounds__(kThreads)
         }
         for (a += t * G; t < nmine; ++t, a += G, b += G) {
           const float4 bv = *b;
-          const float v = plane_weight(c, e, *a, bv, dz, lp, lm, col, rho);
+          const float v = plane_weight<SM>(c, e, *a, bv, dz, lp, lm, col, rho, w);
           if (v != 0.0f) atomicAdd(o + __float_as_int(bv.w), v * inv);
         }
       } else {
         for (int t = 0, i = g0; t < nmine; ++t, i += G, a += G, b += G, cp += kThreads) {
           const float4 bv = *b;
-          const float v = t < ncached ? *cp : plane_weight(c, e, *a, bv, dz, lp, lm, col, rho);
+          const float v =
+              t < ncached ? *cp : plane_weight<SM>(c, e, *a, bv, dz, lp, lm, col, rho, w);
           const float x = v * multiplicity(i, dup, ni - 1);
           if (x != 0.0f) atomicAdd(o + __float_as_int(bv.w), x * inv);
         }
@@ -629,11 +679,12 @@ __global__ void __launch_bounds__(kThreads)
         const int cn = static_cast<int>(nin - cb < kPix ? nin - cb : kPix);
         __syncthreads();
         for (int j = tid; j < cn; j += kThreads)
-          pixel_terms(c, e, s1, p16, w, sens, static_cast<int64_t>(fe.pixel_info_begin) + cb + j,
-                      pa[j], pb[j]);
+          pixel_terms<SM>(c, e, s1, p16, w, sens,
+                          static_cast<int64_t>(fe.pixel_info_begin) + cb + j, pa[j], pb[j]);
         __syncthreads();
         for (int i = i0, k = k0; i < cn; walk(i, k, q, r, npl)) {
-          const float x = voxel_weight(c, e, pa[i], pb[i], k, rho) * multiplicity(cb + i, dup, nin - 1);
+          const float x = voxel_weight<SM>(c, e, pa[i], pb[i], k, rho, w) *
+                          multiplicity(cb + i, dup, nin - 1);
           if (x != 0.0f) atomicAdd(&out[__float_as_int(pb[i].w) + e.plane_begin + k], x * inv);
         }
       }
@@ -714,6 +765,8 @@ HybConst make_const(const jpet_hybrid_geom& g) {
   c.n_planes = g.n_planes;
   c.n_lors = static_cast<int32_t>((static_cast<int64_t>(g.n_detectors) + 1) * g.n_detectors / 2);
   c.n_infos = g.n_pixel_infos;
+  c.n_planes_half = g.n_planes_half > 1 ? g.n_planes_half : 1;
+  c.sens_depth = 1;
   return c;
 }
 
@@ -734,6 +787,10 @@ int check_geom(const jpet_hybrid_geom* g) {
     return fail(nullptr, JPET_ERR_ARGUMENT, "LOR arrays are NULL");
   if (g->n_pixel_infos > 0 && (!g->pixels || !g->pixel_positions))
     return fail(nullptr, JPET_ERR_ARGUMENT, "pixel info arrays are NULL");
+  if (g->n_planes_half < 0 || g->n_planes_half > g->n_planes)
+    return fail(nullptr, JPET_ERR_ARGUMENT, "n_planes_half must be in [0, n_planes]");
+  if (g->n_planes_half > 1 && g->n_pixel_infos * g->n_planes_half >= (int64_t(1) << 31))
+    return fail(nullptr, JPET_ERR_ARGUMENT, "more than 2^31 - 1 weights");
   const int64_t n_lors = (static_cast<int64_t>(g->n_detectors) + 1) * g->n_detectors / 2;
   for (int64_t l = 0; l < n_lors; ++l) {
     if (g->lor_pixel_info_begin[l] > g->lor_pixel_info_end[l] ||
@@ -751,7 +808,8 @@ int check_geom(const jpet_hybrid_geom* g) {
 int sort_and_check_pixels(jpet_hybrid* h, bool sum) {
   const int64_t n = h->c.n_infos;
   const int64_t n_px = static_cast<int64_t>(h->c.n_columns) * h->c.n_rows;
-  HYB_CUDA(h, cudaMemsetAsync(h->sens.p, 0, n_px * sizeof(float), h->stream), "memset");
+  HYB_CUDA(h, cudaMemsetAsync(h->sens.p, 0, n_px * h->c.sens_depth * sizeof(float), h->stream),
+           "memset");
   if (n == 0) return JPET_OK;
   Buf<int32_t> keys2, vals2, lor_of;
   struct Release {
@@ -784,9 +842,13 @@ int sort_and_check_pixels(jpet_hybrid* h, bool sum) {
                                                              h->flag.p);
   HYB_CUDA(h, cudaGetLastError(), "unique pixels");
   if (sum) {
-    sensitivity_sum_kernel<<<grid_for(h, n), 256, 0, h->stream>>>(keys2.p, vals2.p, n, h->w.p,
-                                                                  h->sens.p);
-    HYB_CUDA(h, cudaGetLastError(), "sensitivity");
+    // one plane half after another (calculate_sensitivity sums each
+    // (pixel, plane) over the infos in info order)
+    for (int plane = 0; plane < h->c.n_planes_half; ++plane) {
+      sensitivity_sum_kernel<<<grid_for(h, n), 256, 0, h->stream>>>(
+          keys2.p, vals2.p, n, h->w.p + n * plane, h->sens.p + n_px * plane);
+      HYB_CUDA(h, cudaGetLastError(), "sensitivity");
+    }
   }
   int bad = 0;
   HYB_CUDA(h, cudaMemcpyAsync(&bad, h->flag.p, sizeof bad, cudaMemcpyDeviceToHost, h->stream),
@@ -904,13 +966,27 @@ int jpet_hybrid_create(const jpet_hybrid_geom* g, const jpet_hybrid_opts* opts_i
   jpet_hybrid_opts opts;
   jpet_hybrid_default_opts(&opts);
   if (opts_in) opts = *opts_in;
-  if (opts.weights < 0 || opts.weights > 2 || opts.sensitivity < 0 || opts.sensitivity > 2)
+  if (opts.weights < 0 || opts.weights > 2 || opts.sensitivity < 0 || opts.sensitivity > 3)
     return fail(nullptr, JPET_ERR_ARGUMENT, "unknown weights or sensitivity mode");
+  const int planes_half = g->n_planes_half > 1 ? g->n_planes_half : 1;
+  if (planes_half > 1 && opts.weights == JPET_HYBRID_WEIGHTS_COMPUTED)
+    return fail(nullptr, JPET_ERR_ARGUMENT,
+                "a multi-plane geometry needs given weights (one system matrix per plane half)");
+  if (planes_half > 1 && opts.sensitivity == JPET_HYBRID_SENSITIVITY_GIVEN)
+    return fail(nullptr, JPET_ERR_ARGUMENT,
+                "a multi-plane geometry has a 3D sensitivity (JPET_HYBRID_SENSITIVITY_GIVEN_3D)");
+  // planes of the sensitivity image (reconstruction.h:80-85)
+  const int sens_depth = planes_half > 1 ? planes_half
+                         : opts.sensitivity == JPET_HYBRID_SENSITIVITY_GIVEN_3D ? g->n_planes / 2
+                                                                                : 1;
+  if (sens_depth < 1)
+    return fail(nullptr, JPET_ERR_ARGUMENT, "a 3D sensitivity needs at least 2 planes");
   if (opts.weights != JPET_HYBRID_WEIGHTS_COMPUTED && g->n_pixel_infos > 0 && !g->pixel_weights)
     return fail(nullptr, JPET_ERR_ARGUMENT, "given weights but pixel_weights is NULL");
   if (opts.weights == JPET_HYBRID_WEIGHTS_COMPUTED && !g->lor_widths)
     return fail(nullptr, JPET_ERR_ARGUMENT, "computed weights need lor_widths");
-  if (opts.sensitivity == JPET_HYBRID_SENSITIVITY_GIVEN && !opts.sensitivity_map)
+  if ((opts.sensitivity == JPET_HYBRID_SENSITIVITY_GIVEN ||
+       opts.sensitivity == JPET_HYBRID_SENSITIVITY_GIVEN_3D) && !opts.sensitivity_map)
     return fail(nullptr, JPET_ERR_ARGUMENT, "given sensitivity but sensitivity_map is NULL");
   if (opts.block_threads != 0)
     return fail(nullptr, JPET_ERR_UNSUPPORTED, "the iteration kernel runs 128-thread CTAs");
@@ -918,6 +994,7 @@ int jpet_hybrid_create(const jpet_hybrid_geom* g, const jpet_hybrid_opts* opts_i
   h->opts = opts;
   h->device = opts.device;
   h->c = make_const(*g);
+  h->c.sens_depth = sens_depth;
   auto bail = [&](int code) {
     g_hybrid_error = h->last_error;
     jpet_hybrid_destroy(h);
@@ -934,7 +1011,8 @@ int jpet_hybrid_create(const jpet_hybrid_geom* g, const jpet_hybrid_opts* opts_i
   CREATE_CUDA(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "stream");
   h->stream = h->own_stream;
   int per_sm = 0;
-  CREATE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, iterate_kernel, kThreads, 0),
+  CREATE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, iterate_kernel<kSens2D>,
+                                                            kThreads, 0),
               "occupancy");
   h->iterate_blocks = std::max(1, per_sm) * h->n_sms;
 
@@ -947,10 +1025,10 @@ int jpet_hybrid_create(const jpet_hybrid_geom* g, const jpet_hybrid_opts* opts_i
   CREATE_CUDA(h->ie.alloc(n_lors), "cudaMalloc");
   CREATE_CUDA(h->pix.alloc(2 * std::max<int64_t>(n, 1)), "cudaMalloc");
   CREATE_CUDA(h->pos.alloc(std::max<int64_t>(n, 1)), "cudaMalloc");
-  CREATE_CUDA(h->w.alloc(std::max<int64_t>(n, 1)), "cudaMalloc");
+  CREATE_CUDA(h->w.alloc(std::max<int64_t>(n * planes_half, 1)), "cudaMalloc");
   CREATE_CUDA(h->keys.alloc(std::max<int64_t>(n, 1)), "cudaMalloc");
   CREATE_CUDA(h->vals.alloc(std::max<int64_t>(n, 1)), "cudaMalloc");
-  CREATE_CUDA(h->sens.alloc(n_px), "cudaMalloc");
+  CREATE_CUDA(h->sens.alloc(n_px * sens_depth), "cudaMalloc");
   CREATE_CUDA(h->rho.alloc(n_vox), "cudaMalloc");
   CREATE_CUDA(h->out.alloc(n_vox), "cudaMalloc");
   CREATE_CUDA(h->n_sel.alloc(1), "cudaMalloc");
@@ -979,7 +1057,7 @@ int jpet_hybrid_create(const jpet_hybrid_geom* g, const jpet_hybrid_opts* opts_i
                                 cudaMemcpyHostToDevice, s),
                 "upload");
     if (opts.weights != JPET_HYBRID_WEIGHTS_COMPUTED)
-      CREATE_CUDA(cudaMemcpyAsync(h->w.p, g->pixel_weights, n * sizeof(float),
+      CREATE_CUDA(cudaMemcpyAsync(h->w.p, g->pixel_weights, n * planes_half * sizeof(float),
                                   cudaMemcpyHostToDevice, s),
                   "upload");
   }
@@ -1003,11 +1081,13 @@ int jpet_hybrid_create(const jpet_hybrid_geom* g, const jpet_hybrid_opts* opts_i
   const int rc2 = sort_and_check_pixels(h, opts.sensitivity == JPET_HYBRID_SENSITIVITY_COMPUTED);
   if (rc2 != JPET_OK) return bail(rc2);
   if (opts.sensitivity == JPET_HYBRID_SENSITIVITY_ONE) {
-    fill_kernel<<<grid_for(h, n_px), 256, 0, s>>>(h->sens.p, n_px, 1.0f);
+    fill_kernel<<<grid_for(h, n_px * sens_depth), 256, 0, s>>>(h->sens.p, n_px * sens_depth,
+                                                               1.0f);
     CREATE_CUDA(cudaGetLastError(), "fill");
-  } else if (opts.sensitivity == JPET_HYBRID_SENSITIVITY_GIVEN) {
-    CREATE_CUDA(cudaMemcpyAsync(h->sens.p, opts.sensitivity_map, n_px * sizeof(float),
-                                cudaMemcpyHostToDevice, s),
+  } else if (opts.sensitivity == JPET_HYBRID_SENSITIVITY_GIVEN ||
+             opts.sensitivity == JPET_HYBRID_SENSITIVITY_GIVEN_3D) {
+    CREATE_CUDA(cudaMemcpyAsync(h->sens.p, opts.sensitivity_map,
+                                n_px * sens_depth * sizeof(float), cudaMemcpyHostToDevice, s),
                 "upload");
   }
   h->keys.release();
@@ -1109,8 +1189,8 @@ int jpet_hybrid_get_sensitivity(jpet_hybrid_t* h, float* sens) {
   if (!h || !sens) return fail(h, JPET_ERR_ARGUMENT, "NULL argument");
   HYB_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
   const int64_t n_px = static_cast<int64_t>(h->c.n_columns) * h->c.n_rows;
-  HYB_CUDA(h, cudaMemcpyAsync(sens, h->sens.p, n_px * sizeof(float), cudaMemcpyDeviceToHost,
-                              h->stream),
+  HYB_CUDA(h, cudaMemcpyAsync(sens, h->sens.p, n_px * h->c.sens_depth * sizeof(float),
+                              cudaMemcpyDeviceToHost, h->stream),
            "download");
   HYB_CUDA(h, cudaStreamSynchronize(h->stream), "synchronize");
   return JPET_OK;
@@ -1120,8 +1200,8 @@ int jpet_hybrid_get_weights(jpet_hybrid_t* h, float* w) {
   if (!h || (!w && h->c.n_infos > 0)) return fail(h, JPET_ERR_ARGUMENT, "NULL argument");
   if (h->c.n_infos == 0) return JPET_OK;
   HYB_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
-  HYB_CUDA(h, cudaMemcpyAsync(w, h->w.p, h->c.n_infos * sizeof(float), cudaMemcpyDeviceToHost,
-                              h->stream),
+  HYB_CUDA(h, cudaMemcpyAsync(w, h->w.p, h->c.n_infos * h->c.n_planes_half * sizeof(float),
+                              cudaMemcpyDeviceToHost, h->stream),
            "download");
   HYB_CUDA(h, cudaStreamSynchronize(h->stream), "synchronize");
   return JPET_OK;
@@ -1137,9 +1217,12 @@ int jpet_hybrid_iterate(jpet_hybrid_t* h, int n) {
     HYB_CUDA(h, cudaMemsetAsync(h->counters.p + 2, 0, sizeof(unsigned long long), h->stream),
              "memset");
     if (h->n_events > 0) {
-      iterate_kernel<<<h->iterate_blocks, kThreads, 0, h->stream>>>(
-          h->ev.p, h->n_events, h->seg.p, h->pix.p, h->w.p, h->sens.p, h->rho.p, h->out.p, h->c,
-          h->counters.p + 2);
+      auto* k = h->c.n_planes_half > 1 ? iterate_kernel<kMultiPlane>
+                : h->c.sens_depth > 1  ? iterate_kernel<kSens3D>
+                                       : iterate_kernel<kSens2D>;
+      k<<<h->iterate_blocks, kThreads, 0, h->stream>>>(h->ev.p, h->n_events, h->seg.p, h->pix.p,
+                                                      h->w.p, h->sens.p, h->rho.p, h->out.p,
+                                                      h->c, h->counters.p + 2);
       HYB_CUDA(h, cudaGetLastError(), "iterate");
     }
     std::swap(h->rho, h->out);
@@ -1180,7 +1263,9 @@ int jpet_hybrid_run(const jpet_hybrid_geom* geom, const float* sensitivity,
   jpet_hybrid_default_opts(&o);
   o.device = device;
   o.weights = JPET_HYBRID_WEIGHTS_NORMALIZED;
-  o.sensitivity = JPET_HYBRID_SENSITIVITY_GIVEN;
+  // a multi-plane geometry comes with its 3D sensitivity (depth n_planes_half)
+  o.sensitivity = (geom && geom->n_planes_half > 1) ? JPET_HYBRID_SENSITIVITY_GIVEN_3D
+                                                    : JPET_HYBRID_SENSITIVITY_GIVEN;
   o.sensitivity_map = sensitivity;
   jpet_hybrid_t* h = nullptr;
   int rc = jpet_hybrid_create(geom, &o, &h);

@@ -556,15 +556,19 @@ __global__ void __launch_bounds__(NW * 32, u_min_blocks<NW>()) iterate_union_ker
   if (nb > 0) issue(0, 0, bws[0]);
   if (nb > 1) issue(1, 1, bws[1]);
   for (int i = threadIdx.x; i < c.count; i += NW * 32) S.bw[i] = bws[i];
+  // rho window by asynchronous copies (zero outside the image), so that its
+  // loads overlap with each other and with the first batches' staging
   for (int r = warp; r < t.win_h; r += NW) {
     const int gy = oy + r;
     for (int col = lane; col < pitch; col += 32) {
       const int gx = ox + col;
-      w_rho[r * pitch + col] = (gy < g.n_y && gx < g.n_z) ? rho[gy * g.n_z + gx] : 0.0f;
+      const bool in = gy < g.n_y && gx < g.n_z;
+      cp_async4(&w_rho[r * pitch + col], rho + (in ? gy * g.n_z + gx : 0), in);
       w_out[r * pitch + col] = 0.0f;
       if (ACC == kAccCompensated) w_comp[r * pitch + col] = 0.0f;
     }
   }
+  cp_async_commit();
   for (int i = threadIdx.x; i < 64; i += NW * 32) w_rho[t.win_h * pitch + i] = 0.0f;
   if (threadIdx.x < kUCols) {
     const float cz = fc.kz * g.pixel_width * g.pixel_width;

@@ -19,7 +19,7 @@ from . import capi
 from .hybrid_workloads import FRAME_EVENT_DTYPE, RESPONSE_DTYPE, HybridGeometry
 
 WEIGHTS_COMPUTED, WEIGHTS_GIVEN, WEIGHTS_NORMALIZED = 0, 1, 2
-SENSITIVITY_COMPUTED, SENSITIVITY_ONE, SENSITIVITY_GIVEN = 0, 1, 2
+SENSITIVITY_COMPUTED, SENSITIVITY_ONE, SENSITIVITY_GIVEN, SENSITIVITY_GIVEN_3D = 0, 1, 2, 3
 
 
 class HybGeom(C.Structure):
@@ -43,6 +43,7 @@ class HybGeom(C.Structure):
         ("sigma_z", C.c_float),
         ("sigma_dl", C.c_float),
         ("length", C.c_float),
+        ("n_planes_half", C.c_int32),
     ]
 
 
@@ -116,7 +117,7 @@ def geom_struct(g: HybridGeometry, weights=None) -> tuple[HybGeom, list]:
                                                g.info_end)]
     s = HybGeom(g.n_detectors, g.n_pixel_infos, *[_ptr(a) for a in keep], g.n_columns,
                 g.n_rows, g.pixel_size, g.lower_left_x, g.lower_left_y, g.n_planes, g.z_left,
-                g.sigma_z, g.sigma_dl, g.length)
+                g.sigma_z, g.sigma_dl, g.length, g.n_planes_half)
     return s, keep
 
 
@@ -125,11 +126,16 @@ class HybridError(RuntimeError):
 
 
 class HybridReconstruction:
-    """One reconstruction on one device (the reference's Reconstruction object)."""
+    """One reconstruction on one device (the reference's Reconstruction object).
+    A geometry with n_planes_half > 1 (one system matrix per plane half) has a
+    3D sensitivity of that depth; SENSITIVITY_GIVEN_3D takes the external 3D
+    sensitivity (depth n_planes / 2 for one plane half)."""
 
     def __init__(self, g: HybridGeometry, weights: int = WEIGHTS_COMPUTED,
                  sensitivity: int = SENSITIVITY_COMPUTED, sensitivity_map=None, device: int = 0):
         self.g = g
+        self.sens_depth = (g.n_planes_half if g.n_planes_half > 1
+                           else (g.n_planes // 2 if sensitivity == SENSITIVITY_GIVEN_3D else 1))
         L = _lib()
         gs, self._keep = geom_struct(g)
         smap = None if sensitivity_map is None else np.ascontiguousarray(sensitivity_map,
@@ -212,13 +218,13 @@ class HybridReconstruction:
 
     @property
     def sensitivity(self) -> np.ndarray:
-        out = np.empty(self.g.n_columns * self.g.n_rows, np.float32)
+        out = np.empty(self.sens_depth * self.g.n_columns * self.g.n_rows, np.float32)
         self._check(_lib().jpet_hybrid_get_sensitivity(self.h, _ptr(out)), "get_sensitivity")
         return out
 
     @property
     def weights(self) -> np.ndarray:
-        out = np.empty(self.g.n_pixel_infos, np.float32)
+        out = np.empty(self.g.n_planes_half * self.g.n_pixel_infos, np.float32)
         self._check(_lib().jpet_hybrid_get_weights(self.h, _ptr(out)), "get_weights")
         return out
 

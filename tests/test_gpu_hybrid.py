@@ -44,18 +44,24 @@ def ref():
     return np.load(GOLDEN)
 
 
+CASES = ["computed", "given", "multiplane", "sens3d"]
+
+
 def _modes(ref, tag):
+    """(weights mode, sensitivity mode, sensitivity map, iterations) of a golden case."""
     gi = ref[tag + "_grid"]
     weights = HY.WEIGHTS_GIVEN if gi[4] else HY.WEIGHTS_COMPUTED
+    if tag + "_sens_in" in ref:
+        return weights, HY.SENSITIVITY_GIVEN_3D, ref[tag + "_sens_in"], int(gi[6])
     sens = HY.SENSITIVITY_ONE if gi[5] else HY.SENSITIVITY_COMPUTED
-    return weights, sens, int(gi[6])
+    return weights, sens, None, int(gi[6])
 
 
-@pytest.mark.parametrize("tag", ["computed", "given"])
+@pytest.mark.parametrize("tag", CASES)
 def test_golden_setup_and_frame_events(ref, tag):
     g = H.from_arrays(ref, tag + "_")
-    weights, sens, _ = _modes(ref, tag)
-    with HY.HybridReconstruction(g, weights, sens) as r:
+    weights, sens, smap, _ = _modes(ref, tag)
+    with HY.HybridReconstruction(g, weights, sens, smap) as r:
         w = r.weights
         if weights == HY.WEIGHTS_GIVEN:
             assert np.array_equal(w, ref[tag + "_weights"])
@@ -74,13 +80,13 @@ def test_golden_setup_and_frame_events(ref, tag):
             ref[tag + "_stats"][0])
 
 
-@pytest.mark.parametrize("tag", ["computed", "given"])
+@pytest.mark.parametrize("tag", CASES)
 def test_golden_iterations(ref, tag):
     g = H.from_arrays(ref, tag + "_")
-    weights, sens, n_iter = _modes(ref, tag)
+    weights, sens, smap, n_iter = _modes(ref, tag)
     rhos = ref[tag + "_rho"]
-    with HY.HybridReconstruction(g, weights, sens) as step, \
-            HY.HybridReconstruction(g, weights, sens) as run:
+    with HY.HybridReconstruction(g, weights, sens, smap) as step, \
+            HY.HybridReconstruction(g, weights, sens, smap) as run:
         step << ref[tag + "_responses"]
         run << ref[tag + "_responses"]
         for it in range(n_iter):
@@ -129,6 +135,43 @@ def test_ring96_against_oracle(ring96):
             rho = nxt
     assert max(single) < TOL_STEP, single
     assert max(free) < TOL_FREE, free
+
+
+@pytest.mark.parametrize("form", ["multiplane", "sens3d"])
+def test_ring96_multiplane_and_3d_sensitivity_against_oracle(form):
+    """The multi-plane form (one system matrix per plane half, 3D sensitivity
+    computed per plane half) and the external 3D sensitivity on the 96-detector
+    ring, events at every plane including plane 0 (where both sides clamp the
+    plane the reference would read one past its arrays)."""
+    g, _, _ = H.workload("hybrid-96", weights="given")
+    smap = None
+    if form == "multiplane":
+        g = H.multiplane_weights(g, g.n_planes // 2, seed=21)
+        mode = HY.SENSITIVITY_COMPUTED
+    else:
+        smap = np.random.default_rng(22).uniform(
+            0.5, 1.5, (g.n_planes // 2) * g.n_columns * g.n_rows).astype(np.float32)
+        mode = HY.SENSITIVITY_GIVEN_3D
+    resp = H.responses(g, 40_000, seed=23)
+    w, s = O.hybrid_setup(g, weights_given=True, sens_given=smap)
+    frames = O.hybrid_translate(g, w, resp)
+    assert np.any(frames["plane_begin"] == 0)
+    threads = os.cpu_count() or 1
+    with HY.HybridReconstruction(g, HY.WEIGHTS_GIVEN, mode, smap) as r:
+        assert np.array_equal(r.weights, w) if form == "sens3d" else rel_max(r.weights, w) < 1e-6
+        assert rel_max(r.sensitivity[s > 0], s[s > 0]) < 1e-6
+        r << resp
+        rho = None
+        for it in range(2):
+            nxt, cnt = O.hybrid_mlem(g, w, s, frames, 1, rho, threads=threads)
+            if rho is not None:
+                r.rho = rho
+            r(1)
+            assert rel_l2(r.rho, nxt) < TOL_STEP, it
+            st = r.statistics()
+            assert [st["used_events"], st["used_pixels"], st["used_voxels"]] == list(cnt[:3])
+            assert st["contributing"] == cnt[3]
+            rho = nxt
 
 
 def test_run_entry_point_schedule_and_result(ring96):

@@ -27,7 +27,7 @@ def test_struct_layouts_match_the_reference_types():
     assert H.FRAME_EVENT_DTYPE.itemsize == 48
     assert H.SEGMENT_DTYPE.itemsize == 48
     assert H.RESPONSE_DTYPE.itemsize == 16
-    assert C.sizeof(HY.HybGeom) == 112
+    assert C.sizeof(HY.HybGeom) == 120
 
 
 def test_rejects_bad_geometry_without_device(tiny):
@@ -55,3 +55,24 @@ def test_rejects_bad_modes_without_device(tiny):
     rc, msg = _create(tiny, o)
     assert rc == -1 and "sensitivity_map" in msg
     assert HY._lib().jpet_hybrid_destroy(None) == 0
+
+
+def test_rejects_bad_multiplane_forms_without_device(tiny):
+    """One system matrix per plane half needs given weights and a 3D
+    sensitivity; n_planes_half may not exceed the planes; an external 3D
+    sensitivity needs at least two planes."""
+    mp = H.multiplane_weights(tiny, tiny.n_planes // 2, seed=1)
+    rc, msg = _create(mp)
+    assert rc == -1 and "given weights" in msg
+    smap = np.ones(tiny.n_columns * tiny.n_rows, np.float32)
+    o = HY.HybOpts(0, HY.WEIGHTS_GIVEN, HY.SENSITIVITY_GIVEN, smap.ctypes.data, 0, 0)
+    rc, msg = _create(mp, o)
+    assert rc == -1 and "3D sensitivity" in msg
+    bad = H.HybridGeometry(**{**mp.__dict__, "n_planes_half": tiny.n_planes + 1})
+    o = HY.HybOpts(0, HY.WEIGHTS_GIVEN, HY.SENSITIVITY_ONE, None, 0, 0)
+    rc, msg = _create(bad, o)
+    assert rc == -1 and "n_planes_half" in msg
+    flat = H.HybridGeometry(**{**tiny.__dict__, "n_planes": 1})
+    o = HY.HybOpts(0, HY.WEIGHTS_COMPUTED, HY.SENSITIVITY_GIVEN_3D, smap.ctypes.data, 0, 0)
+    rc, msg = _create(flat, o)
+    assert rc == -1 and "2 planes" in msg
