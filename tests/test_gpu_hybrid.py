@@ -153,6 +153,8 @@ def test_ring96_multiplane_and_3d_sensitivity_against_oracle(form):
             0.5, 1.5, (g.n_planes // 2) * g.n_columns * g.n_rows).astype(np.float32)
         mode = HY.SENSITIVITY_GIVEN_3D
     resp = H.responses(g, 40_000, seed=23)
+    # a thousand of them moved to the grid's first planes
+    resp["z_up"][:1000] = resp["z_dn"][:1000] = g.z_left + 1.5 * g.pixel_size
     w, s = O.hybrid_setup(g, weights_given=True, sens_given=smap)
     frames = O.hybrid_translate(g, w, resp)
     assert np.any(frames["plane_begin"] == 0)
