@@ -223,7 +223,10 @@ int jpet_strip_nll_grad(jpet_strip_t* h, double sigma_z, double sigma_dl, const 
  * the call, so it may overlap neither the input image nor the responses
  * (rejected with JPET_ERR_ARGUMENT).  Work runs on cuda_stream (a cudaStream_t, NULL = the
  * default stream) in the reference's CPU float semantics and operation order;
- * no handle is involved.  The per-event working data live in one fixed 24 MiB
+ * no handle is involved.  It evaluates every box pixel in that order and adds
+ * with global float atomics: on a GB300, 18 ms per iteration of 1048576 events
+ * at 2 mm pixels (sigma 10 / 42 mm), about 17 times the time of a handle's
+ * default kernel, which prepares its events into buffers it allocates.  The per-event working data live in one fixed 24 MiB
  * device array of the library, which every GPU that loads the library keeps
  * until the process exits; calls share it, so calls that overlap on the GPU
  * (different streams or unordered host threads) race, while calls ordered on
