@@ -84,7 +84,8 @@ namespace {
 constexpr int kURows = 64;       // union rows per batch
 constexpr int kUCols = 32;       // union columns from the even start
 constexpr int kUSW = 4;          // sweeps of 8 columns (4 lanes x 2 pixels)
-constexpr int kUMaxChunk = 512;  // events per chunk
+constexpr int kUMaxChunk = 1024;     // events per chunk (batch words keep 10 bits of offset)
+constexpr int kUMaxChunkFixed = 512; // fixed point: a window pixel's integer sum stays < 2^31
 constexpr int kUMaxE = 8;        // largest batch
 constexpr int kUWinRows = 128;   // window rows the batch former tracks (4 per lane)
 // Padded per-event strides of the shared-memory batch arrays: the set-up
@@ -299,7 +300,8 @@ __device__ __forceinline__ void u_forward_chain(float2 (&kr)[E][RS][kUSW], DT (&
 //   kAccFixed        v rounded once to 2^-22 of an event with the batch's
 //                    dither (floor(v 2^22 + U), U uniform in [0, 1): unbiased)
 //                    and added to the integer window (order-independent sums;
-//                    a window pixel of a chunk of <= 512 events stays < 2^31).
+//                    a window pixel of a chunk of <= 512 events stays < 2^31,
+//                    so the fixed-point mode's chunks hold at most 512).
 template <int ACC>
 __device__ __forceinline__ void u_accumulate(float* w_out, float* w_comp, int idx, float2 v,
                                              bool own, float dither) {
@@ -988,7 +990,8 @@ cudaError_t launch_iterate_union(const DevGeom& g, const FastConst& fc, const Ti
                                  AuxImage aux, DevCounters* counters, int precision,
                                  uint32_t seed, cudaStream_t s) {
   if (n_chunks <= 0) return cudaSuccess;
-  if (t.chunk_events > kUMaxChunk || (t.threads != 128 && t.threads != 256))
+  if (t.chunk_events > kUMaxChunk || (t.threads != 128 && t.threads != 256) ||
+      (precision == kPrecisionFixed && t.chunk_events > kUMaxChunkFixed))
     return cudaErrorInvalidValue;
   const int xm = union_chain_exponent(g, fc) ? kXChain
                  : union_split_exponent(g, fc) ? kXSplit
