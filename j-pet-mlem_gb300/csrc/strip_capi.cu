@@ -200,8 +200,8 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
                    Tiling& t) {
   // window pixels per array (rho, out): 12288 (~100 KiB per CTA, 2 CTAs per SM)
   // for 256-thread CTAs; 6144 (~55 KiB, 4 CTAs per SM) for the row-owned
-  // kernel's 128-thread CTAs and for the batch-union kernel (~74 KiB with its
-  // batch records, ~98 KiB with the compensation window, 2 CTAs of 256
+  // kernel's 128-thread CTAs and for the batch-union kernel (~76 KiB with its
+  // batch records, ~100 KiB with the compensation window, 2 CTAs of 256
   // threads per SM)
   const bool fast = o.mode == JPET_MODE_CPU_REFERENCE &&
                     (o.variant == JPET_VARIANT_FAST || o.variant == JPET_VARIANT_ROWS);
