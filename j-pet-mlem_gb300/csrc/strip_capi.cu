@@ -243,10 +243,10 @@ void choose_tiling(const jpet_strip_opts& o, const std::vector<int32_t>& hw,
   t.win_h = th + mh;
   t.n_tiles_x = (n_z + tw - 1) / tw;
   t.n_tiles_y = (n_y + th - 1) / th;
-  // events per chunk: 1024 for the batch-union kernel (half the chunk prologues
-  // and window flushes of 512), 512 for the other kernels and the fixed-point
-  // mode (whose integer window sums must stay below 2^31)
-  t.chunk_events = (union_k && o.precision != JPET_PRECISION_FIXED) ? 1024 : 512;
+  // events per chunk: 2048 for the batch-union kernel (a quarter of the chunk
+  // prologues and window flushes of 512), 512 for the other kernels and the
+  // fixed-point mode (whose integer window sums must stay below 2^31)
+  t.chunk_events = (union_k && o.precision != JPET_PRECISION_FIXED) ? 2048 : 512;
   // the FP32 batch-union kernel (FAST variant) defaults to 256-thread CTAs
   // (8 events per batch); the row-owned kernel to 128
   t.threads = o.block_threads > 0 ? o.block_threads : (union_k ? 256 : (rows4 ? 128 : 256));

@@ -84,7 +84,7 @@ namespace {
 constexpr int kURows = 64;       // union rows per batch
 constexpr int kUCols = 32;       // union columns from the even start
 constexpr int kUSW = 4;          // sweeps of 8 columns (4 lanes x 2 pixels)
-constexpr int kUMaxChunk = 1024;     // events per chunk (batch words keep 10 bits of offset)
+constexpr int kUMaxChunk = 2048;     // events per chunk (batch words keep 11 bits of offset)
 constexpr int kUMaxChunkFixed = 512; // fixed point: a window pixel's integer sum stays < 2^31
 constexpr int kUMaxE = 8;        // largest batch
 constexpr int kUWinRows = 128;   // window rows the batch former tracks (4 per lane)
@@ -105,15 +105,15 @@ struct UEvConst {
 };
 static_assert(sizeof(UEvConst) == 32, "two 16-byte pieces");
 
-// Batch word: first event (offset in the chunk) | events << 10 | union rows << 14
-// | union's first window row << 21.
+// Batch word: first event (offset in the chunk) | events << 11 | union rows << 15
+// | union's first window row << 22.
 __host__ __device__ inline uint32_t ubatch_word(int first, int cnt, int rows, int u0) {
-  return static_cast<uint32_t>(first) | (static_cast<uint32_t>(cnt) << 10) |
-         (static_cast<uint32_t>(rows) << 14) | (static_cast<uint32_t>(u0) << 21);
+  return static_cast<uint32_t>(first) | (static_cast<uint32_t>(cnt) << 11) |
+         (static_cast<uint32_t>(rows) << 15) | (static_cast<uint32_t>(u0) << 22);
 }
-__device__ __forceinline__ int ub_first(uint32_t w) { return static_cast<int>(w & 1023u); }
-__device__ __forceinline__ int ub_cnt(uint32_t w) { return static_cast<int>((w >> 10) & 15u); }
-__device__ __forceinline__ int ub_u0(uint32_t w) { return static_cast<int>((w >> 21) & 127u); }
+__device__ __forceinline__ int ub_first(uint32_t w) { return static_cast<int>(w & 2047u); }
+__device__ __forceinline__ int ub_cnt(uint32_t w) { return static_cast<int>((w >> 11) & 15u); }
+__device__ __forceinline__ int ub_u0(uint32_t w) { return static_cast<int>((w >> 22) & 127u); }
 
 // Union row word (per batch and union row): start column in the window | width << 9.
 __host__ __device__ inline uint16_t urow_word(int u, int wu) {
